@@ -1,0 +1,519 @@
+// capi.cu -- implementation of the C ABI declared in include/fftperm.h.
+//
+// Each entry point orchestrates device-resident state (internal.h) and the
+// kernels of kernels_setup.cu, kernels_fft.cu and kernels_minres.cu.  Host
+// buffers are copied in and out at the boundary; the solve paths keep every
+// vector on the device between the copies.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/fftperm.h"
+#include "internal.h"
+
+struct fp_problem {
+    fp::Problem P;
+};
+
+namespace {
+
+using fp::Problem;
+
+int fail(Problem& P, int code, const std::string& msg) {
+    P.err = msg;
+    return code;
+}
+
+int cuda_fail(Problem& P, cudaError_t e, const char* where) {
+    P.err = std::string(where) + ": " + cudaGetErrorString(e);
+    return FP_ERR_CUDA;
+}
+
+#define FP_CUDA(call, where)                          \
+    do {                                              \
+        cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess) return cuda_fail(P, e_, where); \
+    } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count) {
+    return cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * (count > 0 ? count : 1));
+}
+
+void free_geometry(Problem& P) {
+    cudaFree(P.d_support);
+    cudaFree(P.d_cin);
+    cudaFree(P.d_cout);
+    cudaFree(P.d_b);
+    cudaFree(P.d_x);
+    cudaFree(P.d_z);
+    for (auto& v : P.d_v) cudaFree(v), v = nullptr;
+    for (auto& w : P.d_w) cudaFree(w), w = nullptr;
+    P.d_support = nullptr;
+    P.d_cin = nullptr;
+    P.d_cout = P.d_b = P.d_x = P.d_z = nullptr;
+    P.has_geometry = false;
+}
+
+int need_geometry(Problem& P, const char* who) {
+    if (!P.has_geometry)
+        return fail(P, FP_ERR_STATE, std::string(who) + ": no geometry set (call fp_set_geometry)");
+    if (P.nb == 0)
+        return fail(P, FP_ERR_STATE, std::string(who) + ": support set is empty");
+    return FP_OK;
+}
+
+int alloc_dense(Problem& P) {
+    if (!P.d_dense_in) FP_CUDA(dalloc(&P.d_dense_in, 3 * (size_t)P.n), "cudaMalloc dense");
+    if (!P.d_dense_out) FP_CUDA(dalloc(&P.d_dense_out, 3 * (size_t)P.n), "cudaMalloc dense");
+    return FP_OK;
+}
+
+int ensure_green32(Problem& P) {
+    if (P.d_green32) return FP_OK;
+    FP_CUDA(dalloc(&P.d_green32, 6 * (size_t)P.nh), "cudaMalloc green32");
+    // convert from the FP64 table
+    std::vector<double> h(6 * (size_t)P.nh);
+    FP_CUDA(cudaMemcpy(h.data(), P.d_green64, sizeof(double) * h.size(), cudaMemcpyDeviceToHost),
+            "green copy");
+    std::vector<float> f(h.size());
+    for (size_t i = 0; i < h.size(); ++i) f[i] = (float)h[i];
+    FP_CUDA(cudaMemcpy(P.d_green32, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice),
+            "green copy");
+    return FP_OK;
+}
+
+// y = P_B A_raw P_B x on device compact vectors (src/bignonnet/VariationalOperator.cpp:19-41)
+int device_operator_apply(Problem& P, const double* d_x, double* d_y) {
+    FP_CUDA(fp::launch_sum3(P, d_x, P.nb, P.d_red), "sum");
+    fp::ApplyArgs a;
+    a.src = d_x;
+    a.src_sum = P.d_red;
+    a.dst = d_y;
+    a.src_kind = fp::kSrcCompact;
+    a.dst_kind = fp::kDstCompact;
+    int nparts = 0;
+    FP_CUDA(fp::launch_apply(P, a, &nparts), "apply");
+    FP_CUDA(fp::launch_reduce4(P, nparts, P.d_red + 4), "reduce");
+    FP_CUDA(fp::launch_sub_mean(P, d_y, P.d_red + 4, 1.0), "sub_mean");
+    return FP_OK;
+}
+
+void f0_coefs(const Problem& P, const double g[3], double cf[3], double cs[3]) {
+    // BackgroundForce.cpp:35-36: c_fluid = -1, c_support = -N_F / N_B
+    const double c_support = -(double)P.nf / (double)P.nb;
+    for (int c = 0; c < 3; ++c) {
+        cf[c] = -1.0 * g[c];
+        cs[c] = c_support * g[c];
+    }
+}
+
+// b = -P_B gather(G * f0) on the device (src/bignonnet/VariationalRHS.cpp:15-31)
+int device_build_rhs(Problem& P, const double g[3], double* d_b) {
+    fp::ApplyArgs a;
+    f0_coefs(P, g, a.f0_fluid, a.f0_support);
+    a.dst = d_b;
+    a.src_kind = fp::kSrcF0;
+    a.dst_kind = fp::kDstCompact;
+    int nparts = 0;
+    FP_CUDA(fp::launch_apply(P, a, &nparts), "apply");
+    FP_CUDA(fp::launch_reduce4(P, nparts, P.d_red + 4), "reduce");
+    FP_CUDA(fp::launch_sub_mean(P, d_b, P.d_red + 4, -1.0), "sub_mean");
+    return FP_OK;
+}
+
+// MINRES on device vectors; d_x receives the solution (P.d_x is used as the
+// iterate).  hist_host may be null.
+int device_minres(Problem& P, const double* d_b, const double* d_x0, double tol, long long maxit,
+                  double* hist_host, fp_solver_stats* st) {
+    if (!(tol > 0.0)) return fail(P, FP_ERR_INVALID, "MinresSolver tolerance must be positive");
+    if (maxit + 1 > P.hist_cap) {
+        cudaFree(P.d_hist);
+        P.d_hist = nullptr;
+        FP_CUDA(dalloc(&P.d_hist, (size_t)maxit + 1), "cudaMalloc hist");
+        P.hist_cap = maxit + 1;
+    }
+    FP_CUDA(fp::minres_start(P, d_b, d_x0, tol, maxit), "minres_start");
+    FP_CUDA(cudaMemcpyAsync(P.h_sc, P.d_sc, sizeof(fp::MinresScalars), cudaMemcpyDeviceToHost,
+                            P.stream),
+            "copy");
+    FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+    const int chunk = 16;
+    while (!P.h_sc->done) {
+        for (int i = 0; i < chunk; ++i) FP_CUDA(fp::minres_iteration(P), "minres_iteration");
+        FP_CUDA(cudaMemcpyAsync(P.h_sc, P.d_sc, sizeof(fp::MinresScalars), cudaMemcpyDeviceToHost,
+                                P.stream),
+                "copy");
+        FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+    }
+    const fp::MinresScalars s = *P.h_sc;
+    if (hist_host) {
+        FP_CUDA(cudaMemcpy(hist_host, P.d_hist, sizeof(double) * (size_t)(s.it + 1),
+                           cudaMemcpyDeviceToHost),
+                "hist copy");
+    }
+    if (st) {
+        st->iterations = s.it;
+        st->final_rel_residual = s.rel_res;
+        st->converged = s.converged ? 1 : (s.rel_res <= tol ? 1 : 0);
+        st->refinements = 0;
+    }
+    return FP_OK;
+}
+
+// v = G*(f0 + P_B x) - mean_B(...), avg = <v> over the domain
+// (src/bignonnet/VelocityRecovery.cpp:12-51).  Leaves U + V' in P.d_dense_out.
+int device_recover(Problem& P, const double g[3], const double* d_x, double avg[3], bool keep_field) {
+    int rc = alloc_dense(P);
+    if (rc) return rc;
+    FP_CUDA(fp::launch_sum3(P, d_x, P.nb, P.d_red), "sum");
+    fp::ApplyArgs a;
+    f0_coefs(P, g, a.f0_fluid, a.f0_support);
+    a.src = d_x;
+    a.src_sum = P.d_red;
+    a.dst = P.d_dense_out;
+    a.src_kind = fp::kSrcF0Compact;
+    a.dst_kind = fp::kDstDense;
+    int nparts = 0;
+    FP_CUDA(fp::launch_apply(P, a, &nparts), "apply");
+    FP_CUDA(fp::launch_reduce4(P, nparts, P.d_red + 4), "reduce");  // sums over all voxels
+    FP_CUDA(fp::launch_gather_sum(P, P.d_dense_out, P.d_red + 8), "gather_sum");
+    double h[12];
+    FP_CUDA(cudaMemcpyAsync(h, P.d_red, sizeof(double) * 12, cudaMemcpyDeviceToHost, P.stream),
+            "copy");
+    FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+    double vprime[3];
+    for (int c = 0; c < 3; ++c) {
+        vprime[c] = -(h[8 + c] / (double)P.nb);
+        avg[c] = (h[4 + c] + (double)P.n * vprime[c]) / (double)P.n;
+    }
+    if (keep_field) {
+        double* d_add = P.d_red + 16;
+        FP_CUDA(cudaMemcpyAsync(d_add, vprime, sizeof(double) * 3, cudaMemcpyHostToDevice, P.stream),
+                "copy");
+        FP_CUDA(fp::launch_add_const3(P, P.d_dense_out, d_add), "add");
+        FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+    }
+    return FP_OK;
+}
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+
+}  // namespace
+
+extern "C" {
+
+int fp_create(int nx, int ny, int nz, double voxel_size, double mu, int p_radius, int precision,
+              fp_handle* out) {
+    if (!out) return FP_ERR_INVALID;
+    *out = nullptr;
+    fp_problem* h = new (std::nothrow) fp_problem();
+    if (!h) return FP_ERR_NOMEM;
+    Problem& P = h->P;
+    *out = h;
+    if (nx <= 0 || ny <= 0 || nz <= 0)
+        return fail(P, FP_ERR_INVALID, "Grid dimensions must be positive");
+    if (!(mu > 0.0)) return fail(P, FP_ERR_INVALID, "GreenOperator viscosity must be positive");
+    if (!(voxel_size > 0.0)) return fail(P, FP_ERR_INVALID, "voxel size must be positive");
+    if (precision != FP_PREC_FP64 && precision != FP_PREC_MIXED)
+        return fail(P, FP_ERR_INVALID, "unknown precision mode");
+    P.nx = nx;
+    P.ny = ny;
+    P.nz = nz;
+    P.n = (long long)nx * ny * nz;
+    P.nxh = nx / 2 + 1;
+    P.nrows = (long long)ny * nz;
+    P.nh = (long long)P.nxh * P.nrows;
+    P.h = voxel_size;
+    P.mu = mu;
+    P.p_radius = p_radius < 0 ? 0 : p_radius;
+    P.precision = precision;
+    if (P.n > 2147483647LL) return fail(P, FP_ERR_INVALID, "grid too large (N must fit in int32)");
+    int dev = 0;
+    FP_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    FP_CUDA(cudaDeviceGetAttribute(&P.sm_count, cudaDevAttrMultiProcessorCount, dev), "attr");
+    FP_CUDA(cudaStreamCreateWithFlags(&P.stream, cudaStreamNonBlocking), "stream");
+    std::string err;
+    if (!fp::make_axis_plan(nx, P.px, err) || !fp::make_axis_plan(ny, P.py, err) ||
+        !fp::make_axis_plan(nz, P.pz, err))
+        return fail(P, FP_ERR_UNSUPPORTED, err);
+    FP_CUDA(dalloc(reinterpret_cast<double2**>(&P.d_spec), 3 * (size_t)P.nh), "cudaMalloc spec");
+    FP_CUDA(dalloc(&P.d_green64, 6 * (size_t)P.nh), "cudaMalloc green");
+    const size_t nparts = (size_t)std::max<long long>(fp::kMaxPartials, P.nrows + 64);
+    FP_CUDA(dalloc(&P.d_partials, 4 * nparts), "cudaMalloc partials");
+    FP_CUDA(dalloc(&P.d_red, 64), "cudaMalloc red");
+    FP_CUDA(dalloc(&P.d_sc, 1), "cudaMalloc scalars");
+    FP_CUDA(cudaMallocHost(&P.h_sc, sizeof(fp::MinresScalars)), "cudaMallocHost");
+    FP_CUDA(dalloc(&P.d_row_ptr, (size_t)P.nrows + 1), "cudaMalloc row_ptr");
+    FP_CUDA(dalloc(&P.d_row_cnt, (size_t)P.nrows + 1), "cudaMalloc row_cnt");
+    FP_CUDA(dalloc(&P.d_mask, (size_t)P.n), "cudaMalloc mask");
+    FP_CUDA(fp::launch_green(P), "green precompute");
+    if (precision == FP_PREC_MIXED) {
+        int rc = ensure_green32(P);
+        if (rc) return rc;
+    }
+    return FP_OK;
+}
+
+int fp_destroy(fp_handle h) {
+    if (!h) return FP_OK;
+    Problem& P = h->P;
+    if (P.stream) cudaStreamSynchronize(P.stream);
+    free_geometry(P);
+    fp::free_axis_plan(P.px);
+    fp::free_axis_plan(P.py);
+    fp::free_axis_plan(P.pz);
+    cudaFree(P.d_spec);
+    cudaFree(P.d_green64);
+    cudaFree(P.d_green32);
+    cudaFree(P.d_dense_in);
+    cudaFree(P.d_dense_out);
+    cudaFree(P.d_partials);
+    cudaFree(P.d_red);
+    cudaFree(P.d_sc);
+    cudaFree(P.d_hist);
+    cudaFree(P.d_row_ptr);
+    cudaFree(P.d_row_cnt);
+    cudaFree(P.d_mask);
+    if (P.h_sc) cudaFreeHost(P.h_sc);
+    if (P.stream) cudaStreamDestroy(P.stream);
+    delete h;
+    return FP_OK;
+}
+
+const char* fp_last_error(fp_handle h) { return h ? h->P.err.c_str() : "null handle"; }
+
+void* fp_stream(fp_handle h) { return h ? (void*)h->P.stream : nullptr; }
+
+int fp_synchronize(fp_handle h) {
+    if (!h) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    FP_CUDA(cudaStreamSynchronize(P.stream), "cudaStreamSynchronize");
+    return FP_OK;
+}
+
+int fp_set_precision(fp_handle h, int precision) {
+    if (!h) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    if (precision != FP_PREC_FP64 && precision != FP_PREC_MIXED)
+        return fail(P, FP_ERR_INVALID, "unknown precision mode");
+    if (precision == FP_PREC_MIXED) {
+        int rc = ensure_green32(P);
+        if (rc) return rc;
+    }
+    P.precision = precision;
+    return FP_OK;
+}
+
+int fp_set_geometry(fp_handle h, const uint8_t* fluid_mask, int support_mode, int64_t* nb_out) {
+    if (!h) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    if (!fluid_mask) return fail(P, FP_ERR_INVALID, "BinaryMedium mask must not be null");
+    if (support_mode != FP_SUPPORT_INTERFACE && support_mode != FP_SUPPORT_FULLSOLID)
+        return fail(P, FP_ERR_INVALID, "unknown support mode");
+    free_geometry(P);
+    P.support_mode = support_mode;
+    FP_CUDA(cudaMemcpyAsync(P.d_mask, fluid_mask, (size_t)P.n, cudaMemcpyHostToDevice, P.stream),
+            "mask copy");
+    FP_CUDA(fp::launch_support(P), "support");
+    const size_t m = 3 * (size_t)P.nb;
+    FP_CUDA(dalloc(&P.d_cin, m), "cudaMalloc");
+    FP_CUDA(dalloc(&P.d_cout, m), "cudaMalloc");
+    FP_CUDA(dalloc(&P.d_b, m), "cudaMalloc");
+    FP_CUDA(dalloc(&P.d_x, m), "cudaMalloc");
+    FP_CUDA(dalloc(&P.d_z, m), "cudaMalloc");
+    for (auto& v : P.d_v) FP_CUDA(dalloc(&v, m), "cudaMalloc");
+    for (auto& w : P.d_w) FP_CUDA(dalloc(&w, m), "cudaMalloc");
+    FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+    P.has_geometry = true;
+    if (nb_out) *nb_out = P.nb;
+    return FP_OK;
+}
+
+int fp_get_support(fp_handle h, int64_t* out) {
+    if (!h || !out) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    if (!P.has_geometry) return fail(P, FP_ERR_STATE, "fp_get_support: no geometry set");
+    std::vector<int> tmp((size_t)P.nb);
+    FP_CUDA(cudaMemcpy(tmp.data(), P.d_support, sizeof(int) * tmp.size(), cudaMemcpyDeviceToHost),
+            "copy");
+    for (size_t i = 0; i < tmp.size(); ++i) out[i] = tmp[i];
+    return FP_OK;
+}
+
+int fp_get_green(fp_handle h, double* g6) {
+    if (!h || !g6) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    FP_CUDA(cudaMemcpy(g6, P.d_green64, sizeof(double) * 6 * (size_t)P.nh, cudaMemcpyDeviceToHost),
+            "copy");
+    return FP_OK;
+}
+
+int fp_green_apply(fp_handle h, const double* force_soa, double* velocity_soa) {
+    if (!h || !force_soa || !velocity_soa) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    int rc = alloc_dense(P);
+    if (rc) return rc;
+    FP_CUDA(cudaMemcpyAsync(P.d_dense_in, force_soa, sizeof(double) * 3 * (size_t)P.n,
+                            cudaMemcpyHostToDevice, P.stream),
+            "copy");
+    fp::ApplyArgs a;
+    a.src = P.d_dense_in;
+    a.dst = P.d_dense_out;
+    a.src_kind = fp::kSrcDense;
+    a.dst_kind = fp::kDstDense;
+    int nparts = 0;
+    FP_CUDA(fp::launch_apply(P, a, &nparts), "apply");
+    FP_CUDA(cudaMemcpyAsync(velocity_soa, P.d_dense_out, sizeof(double) * 3 * (size_t)P.n,
+                            cudaMemcpyDeviceToHost, P.stream),
+            "copy");
+    FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+    return FP_OK;
+}
+
+int fp_background_force(fp_handle h, const double grad[3], double* f0_soa) {
+    if (!h || !grad || !f0_soa) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    int rc = need_geometry(P, "fp_background_force");
+    if (rc) return rc;
+    rc = alloc_dense(P);
+    if (rc) return rc;
+    double cf[3], cs[3];
+    f0_coefs(P, grad, cf, cs);
+    FP_CUDA(fp::launch_background_force(P, cf, cs, P.d_dense_out), "f0");
+    FP_CUDA(cudaMemcpyAsync(f0_soa, P.d_dense_out, sizeof(double) * 3 * (size_t)P.n,
+                            cudaMemcpyDeviceToHost, P.stream),
+            "copy");
+    FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+    return FP_OK;
+}
+
+int fp_operator_apply(fp_handle h, const double* x, double* y) {
+    if (!h || !x || !y) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    int rc = need_geometry(P, "VariationalOperator::apply");
+    if (rc) return rc;
+    const size_t bytes = sizeof(double) * 3 * (size_t)P.nb;
+    FP_CUDA(cudaMemcpyAsync(P.d_cin, x, bytes, cudaMemcpyHostToDevice, P.stream), "copy");
+    rc = device_operator_apply(P, P.d_cin, P.d_cout);
+    if (rc) return rc;
+    FP_CUDA(cudaMemcpyAsync(y, P.d_cout, bytes, cudaMemcpyDeviceToHost, P.stream), "copy");
+    FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+    return FP_OK;
+}
+
+int fp_operator_apply_device(fp_handle h, const double* d_x, double* d_y) {
+    if (!h || !d_x || !d_y) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    int rc = need_geometry(P, "VariationalOperator::apply");
+    if (rc) return rc;
+    return device_operator_apply(P, d_x, d_y);
+}
+
+int fp_build_rhs(fp_handle h, const double grad[3], double* b) {
+    if (!h || !grad || !b) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    int rc = need_geometry(P, "VariationalRHS::build");
+    if (rc) return rc;
+    rc = device_build_rhs(P, grad, P.d_b);
+    if (rc) return rc;
+    FP_CUDA(cudaMemcpyAsync(b, P.d_b, sizeof(double) * 3 * (size_t)P.nb, cudaMemcpyDeviceToHost,
+                            P.stream),
+            "copy");
+    FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+    return FP_OK;
+}
+
+int fp_minres(fp_handle h, const double* b, const double* x0, double tol, int64_t maxit,
+              double* x, double* hist, fp_solver_stats* stats) {
+    if (!h || !b || !x) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    int rc = need_geometry(P, "MinresSolver::solve");
+    if (rc) return rc;
+    if (maxit < 0) return fail(P, FP_ERR_INVALID, "max_iterations must be non-negative");
+    const double t0 = now_s();
+    const size_t bytes = sizeof(double) * 3 * (size_t)P.nb;
+    FP_CUDA(cudaMemcpyAsync(P.d_b, b, bytes, cudaMemcpyHostToDevice, P.stream), "copy");
+    if (x0) FP_CUDA(cudaMemcpyAsync(P.d_cin, x0, bytes, cudaMemcpyHostToDevice, P.stream), "copy");
+    rc = device_minres(P, P.d_b, x0 ? P.d_cin : nullptr, tol, maxit, hist, stats);
+    if (rc) return rc;
+    FP_CUDA(cudaMemcpyAsync(x, P.d_x, bytes, cudaMemcpyDeviceToHost, P.stream), "copy");
+    FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+    if (stats) stats->seconds = now_s() - t0;
+    return FP_OK;
+}
+
+int fp_recover(fp_handle h, const double grad[3], const double* x, double* v_soa, double avg[3]) {
+    if (!h || !grad || !x || !avg) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    int rc = need_geometry(P, "VelocityRecovery::recover");
+    if (rc) return rc;
+    FP_CUDA(cudaMemcpyAsync(P.d_cin, x, sizeof(double) * 3 * (size_t)P.nb, cudaMemcpyHostToDevice,
+                            P.stream),
+            "copy");
+    rc = device_recover(P, grad, P.d_cin, avg, v_soa != nullptr);
+    if (rc) return rc;
+    if (v_soa) {
+        FP_CUDA(cudaMemcpy(v_soa, P.d_dense_out, sizeof(double) * 3 * (size_t)P.n,
+                           cudaMemcpyDeviceToHost),
+                "copy");
+    }
+    return FP_OK;
+}
+
+int fp_solve_load_case(fp_handle h, const double grad[3], const double* x0, double tol,
+                       int64_t maxit, double avg[3], double* x_out, fp_solver_stats* stats) {
+    if (!h || !grad || !avg) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    int rc = need_geometry(P, "solve_one_direction");
+    if (rc) return rc;
+    const double t0 = now_s();
+    const size_t bytes = sizeof(double) * 3 * (size_t)P.nb;
+    if (x0) FP_CUDA(cudaMemcpyAsync(P.d_cin, x0, bytes, cudaMemcpyHostToDevice, P.stream), "copy");
+    rc = device_build_rhs(P, grad, P.d_b);
+    if (rc) return rc;
+    fp_solver_stats st{};
+    rc = device_minres(P, P.d_b, x0 ? P.d_cin : nullptr, tol, maxit, nullptr, &st);
+    if (rc) return rc;
+    rc = device_recover(P, grad, P.d_x, avg, false);
+    if (rc) return rc;
+    if (x_out) {
+        FP_CUDA(cudaMemcpyAsync(x_out, P.d_x, bytes, cudaMemcpyDeviceToHost, P.stream), "copy");
+        FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+    }
+    st.seconds = now_s() - t0;
+    if (stats) *stats = st;
+    return FP_OK;
+}
+
+int fp_solve_permeability(fp_handle h, double tol, int64_t maxit, double K[9],
+                          fp_solver_stats stats[3]) {
+    if (!h || !K) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    int rc = need_geometry(P, "PermeabilityRunner::run");
+    if (rc) return rc;
+    for (int col = 0; col < 3; ++col) {
+        double g[3] = {0.0, 0.0, 0.0};
+        g[col] = 1.0;
+        double avg[3];
+        fp_solver_stats st{};
+        rc = fp_solve_load_case(h, g, nullptr, tol, maxit, avg, nullptr, &st);
+        if (rc) return rc;
+        // colK = -mu <v>; set_column stores -colK (PermeabilityRunner.cpp:772-777,
+        // PermeabilityTensor.cpp:16)
+        for (int row = 0; row < 3; ++row) K[row * 3 + col] = -(-P.mu * avg[row]);
+        if (stats) stats[col] = st;
+    }
+    return FP_OK;
+}
+
+}  // extern "C"

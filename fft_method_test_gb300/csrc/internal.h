@@ -1,0 +1,157 @@
+// internal.h -- device-resident state of one permeability problem and the
+// host-side launchers of the CUDA kernels.  Not part of the public C ABI
+// (include/fftperm.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "fft_engine.cuh"
+
+namespace fp {
+
+enum Precision { kFP64 = 0, kMixed = 1 };
+
+struct AxisPlan {
+    FftPlanDev dev{};
+    double2* tw64 = nullptr;
+    float2* tw32 = nullptr;
+};
+
+// Build a plan for length n (factors 2, 3, 5 only); returns false otherwise.
+bool make_axis_plan(int n, AxisPlan& p, std::string& err);
+void free_axis_plan(AxisPlan& p);
+
+// MINRES scalar state on the device (all FP64).  Layout is private.
+struct MinresScalars {
+    double tol;
+    double rhs_norm;
+    double beta;      // beta_k
+    double beta_new;  // beta_{k+1}
+    double alpha;
+    double cs_old, sn_old, cs, sn;
+    double phi_bar;
+    double rel_res;
+    // coefficients of the current iteration's vector update
+    double eps, delta, rho, step, inv_beta_new;
+    double vsum[3];  // component sums of the current Lanczos vector v
+    double zmean[3];
+    long long it;     // completed iterations
+    long long maxit;
+    int done;
+    int converged;
+    int breakdown;
+    int pad;
+};
+
+struct Problem {
+    int nx = 0, ny = 0, nz = 0;
+    long long n = 0;      // voxels
+    int nxh = 0;          // nx/2 + 1
+    long long nh = 0;     // half spectrum points
+    long long nrows = 0;  // ny * nz
+    double h = 1.0, mu = 1.0;
+    int p_radius = 2;
+    int precision = kFP64;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+
+    AxisPlan px, py, pz;
+
+    // geometry
+    uint8_t* d_mask = nullptr;
+    int* d_support = nullptr;    // ascending flat indices (N_B)
+    int* d_row_ptr = nullptr;    // nrows + 1
+    int* d_row_cnt = nullptr;    // scratch: per-row counts
+    long long nb = 0;
+    long long nf = 0;            // fluid voxels
+    int support_mode = 0;
+    bool has_geometry = false;
+
+    // Green tensor on the half spectrum, symmetrised: 6 x nh (xx xy xz yy yz zz)
+    double* d_green64 = nullptr;
+    float* d_green32 = nullptr;
+
+    // spectral work field: 3 x nh complex (double2 or float2)
+    void* d_spec = nullptr;
+
+    // dense real fields for full-grid entry points (3 x n), allocated lazily
+    double* d_dense_in = nullptr;
+    double* d_dense_out = nullptr;
+
+    // compact vectors (3 * nb doubles)
+    double* d_cin = nullptr;
+    double* d_cout = nullptr;
+    double* d_b = nullptr;
+    double* d_x = nullptr;
+    double* d_z = nullptr;
+    double* d_v[3] = {nullptr, nullptr, nullptr};
+    double* d_w[2] = {nullptr, nullptr};
+
+    // reductions
+    double* d_partials = nullptr;  // partial sums (kMaxPartials * 8)
+    double* d_red = nullptr;       // small result slots
+    MinresScalars* d_sc = nullptr;
+    MinresScalars* h_sc = nullptr;  // pinned mirror
+    double* d_hist = nullptr;       // residual history (maxit + 1)
+    long long hist_cap = 0;
+
+    std::string err;
+};
+
+constexpr int kMaxPartials = 8192;
+
+// ---- setup kernels (kernels_setup.cu) ----
+cudaError_t launch_support(Problem& P);
+cudaError_t launch_green(Problem& P);
+
+// ---- operator passes (kernels_fft.cu) ----
+// Source of the forward x pass.
+enum XSource {
+    kSrcCompact = 0,   // scatter compact (3*nb AoS) minus mean
+    kSrcDense = 1,     // dense SoA field (3 x n)
+    kSrcF0 = 2,        // background force f0 only
+    kSrcF0Compact = 3  // f0 plus scattered compact vector minus mean
+};
+// Destination of the inverse x pass.
+enum XDest {
+    kDstCompact = 0,  // gather to compact (raw, not mean-removed) + partial sums
+    kDstDense = 1     // dense SoA field (3 x n) + partial sums over all voxels
+};
+
+struct ApplyArgs {
+    const double* src = nullptr;     // compact or dense source
+    const double* src_sum = nullptr; // device: component sums of the compact source (3), or null
+    double f0_fluid[3] = {0, 0, 0};  // f0 coefficient on fluid voxels (per component)
+    double f0_support[3] = {0, 0, 0};
+    double* dst = nullptr;           // compact or dense destination
+    const double* dot_with = nullptr;  // optional compact vector v: partial dot(v, dst)
+    int src_kind = kSrcCompact;
+    int dst_kind = kDstCompact;
+    const int* skip = nullptr;       // device flag: when nonzero every pass returns at once
+    int precision = -1;              // kFP64 / kMixed; -1 = the problem's default
+};
+
+// Runs the five passes (forward x, y, z + Green + inverse z, inverse y,
+// inverse x).  Writes per-CTA partial sums of the destination into
+// P.d_partials as [blocks][4] = {sum_x, sum_y, sum_z, dot}; returns the number
+// of partial rows in *nparts.
+cudaError_t launch_apply(Problem& P, const ApplyArgs& a, int* nparts);
+
+// ---- vector kernels (kernels_minres.cu) ----
+cudaError_t launch_sum3(Problem& P, const double* v, long long nb, double* out3);
+// Reduce [nparts][4] partials into out4 (deterministic, one block).
+cudaError_t launch_reduce4(Problem& P, int nparts, double* out4);
+cudaError_t minres_start(Problem& P, const double* b, const double* x0, double tol,
+                         long long maxit);
+cudaError_t minres_iteration(Problem& P);
+cudaError_t launch_sub_mean(Problem& P, double* v, const double* sums, double scale);
+cudaError_t launch_gather_sum(Problem& P, const double* u_dense, double* out4);
+cudaError_t launch_add_const3(Problem& P, double* u_dense, const double* add3);
+cudaError_t launch_background_force(Problem& P, const double cf[3], const double cs[3],
+                                    double* f0);
+
+}  // namespace fp

@@ -1,0 +1,502 @@
+// kernels_minres.cu -- MINRES on the device (src/solver/MinresSolver.cpp:46-218).
+//
+// All Lanczos vectors, inner products and the Givens recurrence stay in FP64
+// on the GPU.  One iteration is
+//   apply   z_raw = A_raw v, fused partial sums of z_raw and of v . z_raw
+//   alpha   one CTA: z mean, alpha = v . (z_raw - mean)
+//   zupd    z = (z_raw - mean) - (alpha v + beta v_old), partial |z|^2
+//   scalar  one CTA: beta_new, Givens rotation, phi_bar, residual history,
+//           stop test (the reference's order of operations)
+//   vwupd   v_new = z / beta_new, w_next = (v - eps w_prev - delta w) / rho,
+//           x += (cs_new phi_bar) w_next, partial component sums of v_new
+//   finish  one CTA: component sums of v_new (the next apply's input mean),
+//           iteration counter, stop -> done
+// Kernels return at once when the solve is done, so the host can queue
+// iterations ahead and read the scalar block only every few iterations.
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cmath>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace fp {
+
+namespace {
+
+constexpr int kVecThreads = 256;
+constexpr double kBreakdownEps = 1e-14;
+
+int vec_blocks(const Problem& P, long long m) {
+    long long b = (m + kVecThreads - 1) / kVecThreads;
+    const long long cap = 8LL * (P.sm_count > 0 ? P.sm_count : 152);
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+// partial component sums (and optionally sum of squares) of an AoS vector
+__global__ void k_sum3(const double* __restrict__ v, long long nb, double* partials) {
+    __shared__ double red[4 * 32];
+    double acc[4] = {0, 0, 0, 0};
+    const long long m = 3 * nb;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double x = v[i];
+        const int c = (int)(i % 3);
+        acc[c] += x;
+        acc[3] += x * x;
+    }
+    double out[4];
+    block_sum<4>(acc, red, out);
+    if (threadIdx.x == 0)
+        for (int i = 0; i < 4; ++i) partials[4LL * blockIdx.x + i] = out[i];
+}
+
+__global__ void k_reduce4(const double* __restrict__ partials, int nparts, double* out) {
+    __shared__ double red[4 * 32];
+    double acc[4] = {0, 0, 0, 0};
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x)
+        for (int j = 0; j < 4; ++j) acc[j] += partials[4LL * i + j];
+    double o[4];
+    block_sum<4>(acc, red, o);
+    if (threadIdx.x == 0)
+        for (int j = 0; j < 4; ++j) out[j] = o[j];
+}
+
+// ---- iteration kernels ------------------------------------------------------
+
+__global__ void k_alpha(MinresScalars* sc, const double* __restrict__ partials, int nparts,
+                        double inv_nb) {
+    if (sc->done) return;
+    __shared__ double red[4 * 32];
+    double acc[4] = {0, 0, 0, 0};
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x)
+        for (int j = 0; j < 4; ++j) acc[j] += partials[4LL * i + j];
+    double o[4];
+    block_sum<4>(acc, red, o);
+    if (threadIdx.x == 0) {
+        double corr = 0.0;
+        for (int c = 0; c < 3; ++c) {
+            sc->zmean[c] = o[c] * inv_nb;
+            corr += sc->zmean[c] * sc->vsum[c];
+        }
+        sc->alpha = o[3] - corr;
+    }
+}
+
+__global__ void k_zupd(const MinresScalars* sc, double* __restrict__ z, const double* __restrict__ v,
+                       const double* __restrict__ v_old, long long m, double* partials) {
+    if (sc->done) return;
+    __shared__ double red[32];
+    const double alpha = sc->alpha, beta = sc->beta;
+    const double mz0 = sc->zmean[0], mz1 = sc->zmean[1], mz2 = sc->zmean[2];
+    double acc[1] = {0.0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % 3);
+        const double mz = c == 0 ? mz0 : (c == 1 ? mz1 : mz2);
+        const double zi = (z[i] - mz) - (alpha * v[i] + beta * v_old[i]);
+        z[i] = zi;
+        acc[0] += zi * zi;
+    }
+    double o[1];
+    block_sum<1>(acc, red, o);
+    if (threadIdx.x == 0) partials[blockIdx.x] = o[0];
+}
+
+__global__ void k_scalar(MinresScalars* sc, const double* __restrict__ partials, int nparts,
+                         double* hist) {
+    if (sc->done) return;
+    __shared__ double red[32];
+    double acc[1] = {0.0};
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) acc[0] += partials[i];
+    double o[1];
+    block_sum<1>(acc, red, o);
+    if (threadIdx.x != 0) return;
+    const double beta_new = sqrt(o[0] > 0.0 ? o[0] : 0.0);
+    const double alpha = sc->alpha;
+    const double beta = sc->beta;
+    // MinresSolver.cpp:148-186
+    const double eps = sc->sn_old * beta;
+    const double delta_raw = -sc->cs_old * beta;
+    const double delta = sc->cs * delta_raw + sc->sn * alpha;
+    const double phi = sc->sn * delta_raw - sc->cs * alpha;
+    const double rho = hypot(phi, beta_new);
+    double cs_new = 1.0, sn_new = 0.0;
+    if (rho > kBreakdownEps) {
+        cs_new = phi / rho;
+        sn_new = beta_new / rho;
+    }
+    sc->beta_new = beta_new;
+    sc->eps = eps;
+    sc->delta = delta;
+    sc->rho = rho;
+    sc->step = cs_new * sc->phi_bar;
+    sc->phi_bar *= sn_new;
+    sc->cs_old = sc->cs;
+    sc->sn_old = sc->sn;
+    sc->cs = cs_new;
+    sc->sn = sn_new;
+    sc->beta = beta_new;
+    const double rel = fabs(sc->phi_bar) / sc->rhs_norm;
+    sc->rel_res = rel;
+    const long long k = sc->it + 1;
+    if (hist) hist[k] = rel;
+    if (rel <= sc->tol) {
+        sc->converged = 1;
+        sc->breakdown = 2;  // stop after this iteration's vector update
+    } else if (beta_new < kBreakdownEps) {
+        sc->converged = rel <= sc->tol;
+        sc->breakdown = 2;
+    } else if (k >= sc->maxit) {
+        sc->breakdown = 2;
+    }
+}
+
+__global__ void k_vwupd(const MinresScalars* sc, const double* __restrict__ z, const double* __restrict__ v,
+                        double* __restrict__ v_new, double* __restrict__ w_prev_to_next,
+                        const double* __restrict__ w, double* __restrict__ x, long long m,
+                        double* partials) {
+    if (sc->done) return;
+    __shared__ double red[4 * 32];
+    const double beta_new = sc->beta_new, eps = sc->eps, delta = sc->delta, rho = sc->rho;
+    const double step = sc->step;
+    const bool vb = beta_new > kBreakdownEps;
+    const bool rb = rho > kBreakdownEps;
+    double acc[4] = {0, 0, 0, 0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double vo = v[i];  // becomes v_old
+        const double vn = vb ? z[i] / beta_new : 0.0;
+        v_new[i] = vn;
+        const double wn = rb ? (vo - eps * w_prev_to_next[i] - delta * w[i]) / rho : 0.0;
+        w_prev_to_next[i] = wn;
+        x[i] += step * wn;
+        acc[(int)(i % 3)] += vn;
+    }
+    double o[4];
+    block_sum<4>(acc, red, o);
+    if (threadIdx.x == 0)
+        for (int j = 0; j < 4; ++j) partials[4LL * blockIdx.x + j] = o[j];
+}
+
+__global__ void k_finish(MinresScalars* sc, const double* __restrict__ partials, int nparts) {
+    if (sc->done) return;
+    __shared__ double red[4 * 32];
+    double acc[4] = {0, 0, 0, 0};
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x)
+        for (int j = 0; j < 4; ++j) acc[j] += partials[4LL * i + j];
+    double o[4];
+    block_sum<4>(acc, red, o);
+    if (threadIdx.x == 0) {
+        for (int c = 0; c < 3; ++c) sc->vsum[c] = o[c];
+        sc->it += 1;
+        if (sc->breakdown == 2) sc->done = 1;
+    }
+}
+
+// ---- start-up kernels -------------------------------------------------------
+
+__global__ void k_start_norms(MinresScalars* sc, const double* __restrict__ partials, int nparts,
+                              int which) {
+    __shared__ double red[4 * 32];
+    double acc[4] = {0, 0, 0, 0};
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x)
+        for (int j = 0; j < 4; ++j) acc[j] += partials[4LL * i + j];
+    double o[4];
+    block_sum<4>(acc, red, o);
+    if (threadIdx.x == 0) {
+        const double nrm = sqrt(o[3] > 0.0 ? o[3] : 0.0);
+        if (which == 0) {
+            sc->rhs_norm = nrm;  // raw |b|, clamped below
+        } else {
+            sc->beta = nrm;  // beta1 = |r0|
+        }
+    }
+}
+
+// r0 = b - (A x0 - mean) when have_x0, else b.
+__global__ void k_residual0(const MinresScalars* sc, const double* __restrict__ b,
+                            double* __restrict__ z, const double* __restrict__ zmean3,
+                            long long m, int have_x0) {
+    const double m0 = have_x0 ? zmean3[0] : 0.0, m1 = have_x0 ? zmean3[1] : 0.0,
+                 m2 = have_x0 ? zmean3[2] : 0.0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+         i += (long long)gridDim.x * blockDim.x) {
+        if (have_x0) {
+            const int c = (int)(i % 3);
+            const double mz = c == 0 ? m0 : (c == 1 ? m1 : m2);
+            z[i] = b[i] - (z[i] - mz);
+        } else {
+            z[i] = b[i];
+        }
+    }
+}
+
+__global__ void k_scale_div(const double* __restrict__ z, double* __restrict__ v,
+                            const MinresScalars* sc, long long m) {
+    const double beta = sc->beta;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+         i += (long long)gridDim.x * blockDim.x)
+        v[i] = z[i] / beta;
+}
+
+__global__ void k_zmean_from_partials(const double* __restrict__ partials, int nparts,
+                                      double inv_nb, double* out3) {
+    __shared__ double red[4 * 32];
+    double acc[4] = {0, 0, 0, 0};
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x)
+        for (int j = 0; j < 4; ++j) acc[j] += partials[4LL * i + j];
+    double o[4];
+    block_sum<4>(acc, red, o);
+    if (threadIdx.x == 0)
+        for (int c = 0; c < 3; ++c) out3[c] = o[c] * inv_nb;
+}
+
+}  // namespace
+
+cudaError_t launch_sum3(Problem& P, const double* v, long long nb, double* out4) {
+    const int blocks = vec_blocks(P, 3 * nb);
+    k_sum3<<<blocks, kVecThreads, 0, P.stream>>>(v, nb, P.d_partials);
+    k_reduce4<<<1, 256, 0, P.stream>>>(P.d_partials, blocks, out4);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce4(Problem& P, int nparts, double* out4) {
+    k_reduce4<<<1, 512, 0, P.stream>>>(P.d_partials, nparts, out4);
+    return cudaGetLastError();
+}
+
+// Host-side iteration counter of the queued iterations (selects the rotating
+// Lanczos/w buffers); reset by minres_start.
+static thread_local long long g_queued = 0;
+
+cudaError_t minres_start(Problem& P, const double* b, const double* x0, double tol,
+                         long long maxit) {
+    const long long m = 3 * P.nb;
+    MinresScalars init{};
+    init.tol = tol;
+    init.maxit = maxit;
+    init.cs_old = -1.0;
+    init.sn_old = 0.0;
+    init.cs = -1.0;
+    init.sn = 0.0;
+    g_queued = 0;
+    cudaError_t e = cudaMemcpyAsync(P.d_sc, &init, sizeof(init), cudaMemcpyHostToDevice, P.stream);
+    if (e != cudaSuccess) return e;
+    const int blocks = vec_blocks(P, m);
+    // |b|
+    k_sum3<<<blocks, kVecThreads, 0, P.stream>>>(b, P.nb, P.d_partials);
+    k_start_norms<<<1, 256, 0, P.stream>>>(P.d_sc, P.d_partials, blocks, 0);
+    // x = x0 or 0
+    if (x0) {
+        cudaMemcpyAsync(P.d_x, x0, sizeof(double) * m, cudaMemcpyDeviceToDevice, P.stream);
+        // z_raw = A_raw x0 with input mean removal
+        launch_sum3(P, P.d_x, P.nb, P.d_red);
+        ApplyArgs a;
+        a.src = P.d_x;
+        a.src_sum = P.d_red;
+        a.dst = P.d_z;
+        a.src_kind = kSrcCompact;
+        a.dst_kind = kDstCompact;
+        int nparts = 0;
+        e = launch_apply(P, a, &nparts);
+        if (e != cudaSuccess) return e;
+        k_zmean_from_partials<<<1, 512, 0, P.stream>>>(P.d_partials, nparts, 1.0 / (double)P.nb,
+                                                       P.d_red + 4);
+        k_residual0<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, b, P.d_z, P.d_red + 4, m, 1);
+    } else {
+        cudaMemsetAsync(P.d_x, 0, sizeof(double) * m, P.stream);
+        k_residual0<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, b, P.d_z, nullptr, m, 0);
+    }
+    // beta1 = |r0|
+    k_sum3<<<blocks, kVecThreads, 0, P.stream>>>(P.d_z, P.nb, P.d_partials);
+    k_start_norms<<<1, 256, 0, P.stream>>>(P.d_sc, P.d_partials, blocks, 1);
+    e = cudaMemcpyAsync(P.h_sc, P.d_sc, sizeof(MinresScalars), cudaMemcpyDeviceToHost, P.stream);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(P.stream);
+    if (e != cudaSuccess) return e;
+    MinresScalars s = *P.h_sc;
+    const double rhs_raw = s.rhs_norm;
+    if (rhs_raw == 0.0) {  // MinresSolver.cpp:76-82
+        s.rhs_norm = DBL_MIN;
+        s.converged = 1;
+        s.done = 1;
+        s.rel_res = 0.0;
+        const double z0 = 0.0;
+        if (P.d_hist) cudaMemcpyAsync(P.d_hist, &z0, sizeof(double), cudaMemcpyHostToDevice, P.stream);
+        *P.h_sc = s;
+        return cudaMemcpyAsync(P.d_sc, P.h_sc, sizeof(MinresScalars), cudaMemcpyHostToDevice, P.stream);
+    }
+    s.rhs_norm = rhs_raw > DBL_MIN ? rhs_raw : DBL_MIN;
+    const double beta1 = s.beta;
+    const double rel0 = beta1 / s.rhs_norm;
+    s.rel_res = rel0;
+    if (P.d_hist) {
+        P.h_sc->rel_res = rel0;  // staging through pinned memory
+        cudaMemcpyAsync(P.d_hist, &P.h_sc->rel_res, sizeof(double), cudaMemcpyHostToDevice, P.stream);
+        cudaStreamSynchronize(P.stream);
+    }
+    if (rel0 <= tol || beta1 == 0.0) {
+        s.converged = 1;
+        s.done = 1;
+        *P.h_sc = s;
+        return cudaMemcpyAsync(P.d_sc, P.h_sc, sizeof(MinresScalars), cudaMemcpyHostToDevice, P.stream);
+    }
+    s.phi_bar = beta1;
+    if (maxit <= 0) s.done = 1;
+    *P.h_sc = s;
+    cudaMemcpyAsync(P.d_sc, P.h_sc, sizeof(MinresScalars), cudaMemcpyHostToDevice, P.stream);
+    // v = r0 / beta1 into V[0]; v_old = V[2] = 0; w = 0
+    k_scale_div<<<blocks, kVecThreads, 0, P.stream>>>(P.d_z, P.d_v[0], P.d_sc, m);
+    cudaMemsetAsync(P.d_v[2], 0, sizeof(double) * m, P.stream);
+    cudaMemsetAsync(P.d_w[0], 0, sizeof(double) * m, P.stream);
+    cudaMemsetAsync(P.d_w[1], 0, sizeof(double) * m, P.stream);
+    // component sums of v (input mean of the first apply)
+    k_sum3<<<blocks, kVecThreads, 0, P.stream>>>(P.d_v[0], P.nb, P.d_partials);
+    k_reduce4<<<1, 256, 0, P.stream>>>(P.d_partials, blocks, P.d_red + 8);
+    // copy the three sums into sc->vsum
+    cudaMemcpyAsync(&P.d_sc->vsum[0], P.d_red + 8, sizeof(double) * 3, cudaMemcpyDeviceToDevice,
+                    P.stream);
+    return cudaGetLastError();
+}
+
+cudaError_t minres_iteration(Problem& P) {
+    const long long m = 3 * P.nb;
+    const long long k = g_queued++;
+    double* v = P.d_v[k % 3];
+    double* v_old = P.d_v[(k + 2) % 3];
+    double* v_new = P.d_v[(k + 1) % 3];
+    double* w_prev = P.d_w[k % 2];
+    double* w = P.d_w[(k + 1) % 2];
+    ApplyArgs a;
+    a.src = v;
+    a.src_sum = &P.d_sc->vsum[0];
+    a.dst = P.d_z;
+    a.dot_with = v;
+    a.src_kind = kSrcCompact;
+    a.dst_kind = kDstCompact;
+    a.skip = &P.d_sc->done;
+    int nparts = 0;
+    cudaError_t e = launch_apply(P, a, &nparts);
+    if (e != cudaSuccess) return e;
+    const double inv_nb = 1.0 / (double)P.nb;
+    k_alpha<<<1, 512, 0, P.stream>>>(P.d_sc, P.d_partials, nparts, inv_nb);
+    const int blocks = vec_blocks(P, m);
+    k_zupd<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, P.d_z, v, v_old, m, P.d_partials);
+    k_scalar<<<1, 256, 0, P.stream>>>(P.d_sc, P.d_partials, blocks, P.d_hist);
+    k_vwupd<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, P.d_z, v, v_new, w_prev, w, P.d_x, m,
+                                                   P.d_partials);
+    k_finish<<<1, 256, 0, P.stream>>>(P.d_sc, P.d_partials, blocks);
+    return cudaGetLastError();
+}
+
+}  // namespace fp
+
+namespace fp {
+
+namespace {
+
+// v = scale * (v - mean), mean = sums[c] * inv_nb (AoS components)
+__global__ void k_sub_mean(double* __restrict__ v, long long m, const double* __restrict__ sums,
+                           double inv_nb, double scale) {
+    const double m0 = sums[0] * inv_nb, m1 = sums[1] * inv_nb, m2 = sums[2] * inv_nb;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % 3);
+        const double mz = c == 0 ? m0 : (c == 1 ? m1 : m2);
+        const double r = v[i] - mz;
+        v[i] = scale == 1.0 ? r : scale * r;
+    }
+}
+
+// sums over the support of a dense SoA field, per component
+__global__ void k_gather_sum(const double* __restrict__ u, long long n, const int* __restrict__ support,
+                             long long nb, double* partials) {
+    __shared__ double red[4 * 32];
+    double acc[4] = {0, 0, 0, 0};
+    for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < nb;
+         s += (long long)gridDim.x * blockDim.x) {
+        const long long v = support[s];
+        acc[0] += u[v];
+        acc[1] += u[n + v];
+        acc[2] += u[2 * n + v];
+    }
+    double o[4];
+    block_sum<4>(acc, red, o);
+    if (threadIdx.x == 0)
+        for (int j = 0; j < 4; ++j) partials[4LL * blockIdx.x + j] = o[j];
+}
+
+// u[c] += add[c] on a dense SoA field
+__global__ void k_add_const3(double* __restrict__ u, long long n, const double* __restrict__ add) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < 3 * n;
+         i += (long long)gridDim.x * blockDim.x) {
+        u[i] += add[i / n];
+    }
+}
+
+// f0 on a dense SoA field (src/bignonnet/BackgroundForce.cpp:14-60)
+__global__ void k_background_force(const uint8_t* __restrict__ mask, long long n,
+                                   const int* __restrict__ support, long long nb, double cf0,
+                                   double cf1, double cf2, double cs0, double cs1, double cs2,
+                                   double* __restrict__ f0) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const bool fl = mask[i] != 0;
+        f0[i] = fl ? cf0 : 0.0;
+        f0[n + i] = fl ? cf1 : 0.0;
+        f0[2 * n + i] = fl ? cf2 : 0.0;
+    }
+    (void)support;
+    (void)nb;
+    (void)cs0;
+    (void)cs1;
+    (void)cs2;
+}
+
+__global__ void k_background_force_support(const int* __restrict__ support, long long nb, long long n,
+                                           double cs0, double cs1, double cs2, double* __restrict__ f0) {
+    for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < nb;
+         s += (long long)gridDim.x * blockDim.x) {
+        const long long v = support[s];
+        f0[v] += cs0;
+        f0[n + v] += cs1;
+        f0[2 * n + v] += cs2;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_sub_mean(Problem& P, double* v, const double* sums, double scale) {
+    const long long m = 3 * P.nb;
+    k_sub_mean<<<vec_blocks(P, m), kVecThreads, 0, P.stream>>>(
+        v, m, sums, P.nb > 0 ? 1.0 / (double)P.nb : 0.0, scale);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_sum(Problem& P, const double* u_dense, double* out4) {
+    const int blocks = vec_blocks(P, P.nb);
+    k_gather_sum<<<blocks, kVecThreads, 0, P.stream>>>(u_dense, P.n, P.d_support, P.nb,
+                                                        P.d_partials);
+    k_reduce4<<<1, 512, 0, P.stream>>>(P.d_partials, blocks, out4);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_add_const3(Problem& P, double* u_dense, const double* add3) {
+    k_add_const3<<<vec_blocks(P, 3 * P.n), kVecThreads, 0, P.stream>>>(u_dense, P.n, add3);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_background_force(Problem& P, const double cf[3], const double cs[3],
+                                    double* f0) {
+    k_background_force<<<vec_blocks(P, P.n), kVecThreads, 0, P.stream>>>(
+        P.d_mask, P.n, P.d_support, P.nb, cf[0], cf[1], cf[2], cs[0], cs[1], cs[2], f0);
+    k_background_force_support<<<vec_blocks(P, P.nb), kVecThreads, 0, P.stream>>>(
+        P.d_support, P.nb, P.n, cs[0], cs[1], cs[2], f0);
+    return cudaGetLastError();
+}
+
+}  // namespace fp

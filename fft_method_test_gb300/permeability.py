@@ -1,0 +1,326 @@
+"""Python host mirror of the reference's operator/solver interfaces, over the
+C ABI (include/fftperm.h).  Names, argument meaning and errors follow the
+reference so that a test written against the reference reads the same here:
+
+=====================================  ==========================================
+reference (C++)                        here
+=====================================  ==========================================
+ForceSupport (ForceSupport.cpp:9-25)   ``PermeabilityProblem.set_geometry`` /
+                                       ``ForceSupport``
+BackgroundForce::build                 ``BackgroundForce.build``
+GreenOperator::apply                   ``GreenOperator.apply``
+VariationalOperator (ILinearOperator)  ``VariationalOperator.size`` / ``.apply``
+VariationalRHS::build                  ``VariationalRHS.build``
+MinresSolver::solve -> SolverResult    ``MinresSolver.solve`` -> ``SolverResult``
+VelocityRecovery::recover              ``VelocityRecovery.recover`` /
+                                       ``.average_over_domain``
+solve_one_direction + K assembly       ``PermeabilityProblem.solve_load_case`` /
+                                       ``.solve_permeability``
+=====================================  ==========================================
+
+Arrays: masks and fields are numpy arrays shaped (nz, ny, nx) (x fastest, the
+reference's flat index); vector fields are (3, nz, ny, nx); compact support
+vectors are flat [3*local + comp].
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _capi
+
+PRECISIONS = {"fp64": _capi.FP_PREC_FP64, "mixed": _capi.FP_PREC_MIXED}
+SUPPORT_MODES = {"interface": _capi.FP_SUPPORT_INTERFACE, "fullsolid": _capi.FP_SUPPORT_FULLSOLID}
+
+
+@dataclass
+class SolverResult:
+    """src/solver/SolverResult.hpp:10-16"""
+    solution: np.ndarray
+    converged: bool = False
+    iterations: int = 0
+    final_rel_residual: float = 1.0
+    residual_history: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    seconds: float = 0.0
+    refinements: int = 0
+
+
+class PermeabilityProblem:
+    """One periodic grid with its device-resident solver state (an fp_handle)."""
+
+    def __init__(self, shape, voxel_size: float = 1.0, mu: float = 1.0, p_radius: int = 2,
+                 precision: str = "fp64"):
+        self.lib = _capi.load()
+        nz, ny, nx = (shape, shape, shape) if np.isscalar(shape) else tuple(shape)
+        self.shape = (int(nz), int(ny), int(nx))
+        self.mu = float(mu)
+        self.voxel_size = float(voxel_size)
+        self.p_radius = int(p_radius)
+        h = C.c_void_p()
+        rc = self.lib.fp_create(int(nx), int(ny), int(nz), float(voxel_size), float(mu),
+                                int(p_radius), PRECISIONS[precision], C.byref(h))
+        self._h = h
+        if rc != _capi.FP_OK:
+            try:
+                _capi.check(self.lib, h, rc)
+            finally:
+                self.close()
+        self.nb = 0
+        self.n = int(nx) * int(ny) * int(nz)
+
+    # -- lifetime ----------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self.lib.fp_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc):
+        _capi.check(self.lib, self._h, rc)
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- configuration -----------------------------------------------------
+    def set_precision(self, precision: str):
+        self._check(self.lib.fp_set_precision(self._h, PRECISIONS[precision]))
+
+    def set_geometry(self, fluid_mask: np.ndarray, support: str = "interface") -> int:
+        m = np.ascontiguousarray(fluid_mask, dtype=np.uint8)
+        if m.shape != self.shape:
+            raise ValueError("BinaryMedium mask size must match grid size")
+        nb = C.c_int64(0)
+        self._check(self.lib.fp_set_geometry(self._h, m.ravel(), SUPPORT_MODES[support],
+                                             C.byref(nb)))
+        self.nb = int(nb.value)
+        return self.nb
+
+    def support(self) -> np.ndarray:
+        out = np.zeros(max(self.nb, 1), dtype=np.int64)
+        self._check(self.lib.fp_get_support(self._h, out))
+        return out[: self.nb]
+
+    def green_tensor(self) -> np.ndarray:
+        nz, ny, nx = self.shape
+        g = np.zeros(6 * nz * ny * (nx // 2 + 1))
+        self._check(self.lib.fp_get_green(self._h, g))
+        return g.reshape(6, nz, ny, nx // 2 + 1)
+
+    # -- operators -----------------------------------------------------------
+    def green_apply(self, force: np.ndarray) -> np.ndarray:
+        f = np.ascontiguousarray(force, dtype=np.float64)
+        if f.size != 3 * self.n:
+            raise ValueError("GreenOperator::apply grid mismatch")
+        u = np.zeros(3 * self.n)
+        self._check(self.lib.fp_green_apply(self._h, f.ravel(), u))
+        return u.reshape((3,) + self.shape)
+
+    def background_force(self, grad) -> np.ndarray:
+        f0 = np.zeros(3 * self.n)
+        self._check(self.lib.fp_background_force(self._h, np.asarray(grad, np.float64), f0))
+        return f0.reshape((3,) + self.shape)
+
+    def operator_apply(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+        if x.size != 3 * self.nb:
+            raise ValueError("VariationalOperator::apply input size mismatch")
+        y = np.zeros(3 * self.nb)
+        self._check(self.lib.fp_operator_apply(self._h, x, y))
+        return y
+
+    def build_rhs(self, grad) -> np.ndarray:
+        b = np.zeros(3 * self.nb)
+        self._check(self.lib.fp_build_rhs(self._h, np.asarray(grad, np.float64), b))
+        return b
+
+    def minres(self, b, tol: float, maxit: int, x0=None, history: bool = True) -> SolverResult:
+        b = np.ascontiguousarray(b, dtype=np.float64).ravel()
+        if b.size != 3 * self.nb:
+            raise ValueError("MinresSolver::solve rhs size mismatch")
+        x = np.zeros(3 * self.nb)
+        hist = np.zeros(maxit + 1) if history else None
+        st = _capi.SolverStats()
+        x0p = None
+        if x0 is not None:
+            x0 = np.ascontiguousarray(x0, dtype=np.float64).ravel()
+            if x0.size != 3 * self.nb:
+                raise ValueError("MinresSolver::solve initial guess size mismatch")
+            x0p = x0.ctypes.data
+        self._check(self.lib.fp_minres(self._h, b, x0p, float(tol), int(maxit), x,
+                                       hist.ctypes.data if history else None, C.byref(st)))
+        d = st.as_dict()
+        return SolverResult(solution=x, converged=d["converged"], iterations=d["iterations"],
+                            final_rel_residual=d["final_rel_residual"],
+                            residual_history=(hist[: d["iterations"] + 1] if history else np.zeros(0)),
+                            seconds=d["seconds"], refinements=d["refinements"])
+
+    def recover(self, grad, x, want_field: bool = False):
+        x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+        if x.size != 3 * self.nb:
+            raise ValueError("VelocityRecovery::recover compact solution size mismatch")
+        avg = np.zeros(3)
+        v = np.zeros(3 * self.n) if want_field else None
+        self._check(self.lib.fp_recover(self._h, np.asarray(grad, np.float64), x,
+                                        v.ctypes.data if want_field else None, avg))
+        return avg, (v.reshape((3,) + self.shape) if want_field else None)
+
+    def solve_load_case(self, grad, tol: float, maxit: int, x0=None, want_solution: bool = False):
+        avg = np.zeros(3)
+        st = _capi.SolverStats()
+        x0p = None
+        if x0 is not None:
+            x0 = np.ascontiguousarray(x0, dtype=np.float64).ravel()
+            x0p = x0.ctypes.data
+        xo = np.zeros(3 * self.nb) if want_solution else None
+        self._check(self.lib.fp_solve_load_case(self._h, np.asarray(grad, np.float64), x0p,
+                                                float(tol), int(maxit), avg,
+                                                xo.ctypes.data if want_solution else None,
+                                                C.byref(st)))
+        return avg, st.as_dict(), xo
+
+    def solve_permeability(self, tol: float, maxit: int):
+        K = np.zeros(9)
+        stats = (_capi.SolverStats * 3)()
+        self._check(self.lib.fp_solve_permeability(self._h, float(tol), int(maxit), K, stats))
+        return K.reshape(3, 3), [s.as_dict() for s in stats]
+
+
+# ---------------------------------------------------------------------------
+# Reference-named facades
+# ---------------------------------------------------------------------------
+
+class ForceSupport:
+    """src/bignonnet/ForceSupport.hpp:12-31 over a PermeabilityProblem."""
+
+    def __init__(self, problem: PermeabilityProblem, fluid_mask, mode: str = "interface"):
+        self.problem = problem
+        problem.set_geometry(fluid_mask, mode)
+        self._active = problem.support()
+        self._local = {int(v): i for i, v in enumerate(self._active)}
+
+    def size(self) -> int:
+        return 3 * len(self._active)
+
+    def num_active_voxels(self) -> int:
+        return len(self._active)
+
+    def active_voxels(self) -> np.ndarray:
+        return self._active
+
+    def contains_voxel(self, voxel: int) -> bool:
+        return int(voxel) in self._local
+
+    def local_index(self, voxel: int) -> int:
+        if int(voxel) not in self._local:
+            raise IndexError("Voxel is not in active support")
+        return self._local[int(voxel)]
+
+    def global_index(self, local: int) -> int:
+        if not 0 <= local < len(self._active):
+            raise IndexError("Support local index out of range")
+        return int(self._active[local])
+
+
+class GreenOperator:
+    """src/bignonnet/GreenOperator.hpp:13-44: apply(force) -> velocity-like field."""
+
+    def __init__(self, problem: PermeabilityProblem):
+        self.problem = problem
+
+    def apply(self, force: np.ndarray) -> np.ndarray:
+        return self.problem.green_apply(force)
+
+
+class BackgroundForce:
+    """src/bignonnet/BackgroundForce.hpp:10-19."""
+
+    def __init__(self, problem: PermeabilityProblem):
+        self.problem = problem
+
+    def build(self, grad) -> np.ndarray:
+        return self.problem.background_force(grad)
+
+
+class VariationalOperator:
+    """The ILinearOperator of the method (src/bignonnet/VariationalOperator.hpp:10-26)."""
+
+    def __init__(self, problem: PermeabilityProblem):
+        self.problem = problem
+
+    def size(self) -> int:
+        return 3 * self.problem.nb
+
+    def apply(self, x) -> np.ndarray:
+        return self.problem.operator_apply(x)
+
+
+class VariationalRHS:
+    """src/bignonnet/VariationalRHS.hpp:11-26."""
+
+    def __init__(self, problem: PermeabilityProblem):
+        self.problem = problem
+
+    def build(self, grad) -> np.ndarray:
+        return self.problem.build_rhs(grad)
+
+
+class MinresSolver:
+    """src/solver/MinresSolver.hpp:11-30; the iteration runs on the GPU."""
+
+    def __init__(self, tolerance: float, max_iterations: int):
+        if not tolerance > 0:
+            raise ValueError("MinresSolver tolerance must be positive")
+        self.tolerance = float(tolerance)
+        self.max_iterations = int(max_iterations)
+
+    def solve(self, op: VariationalOperator, rhs, initial_guess=None) -> SolverResult:
+        return op.problem.minres(rhs, self.tolerance, self.max_iterations, x0=initial_guess)
+
+
+class VelocityRecovery:
+    """src/bignonnet/VelocityRecovery.hpp:13-29."""
+
+    def __init__(self, problem: PermeabilityProblem):
+        self.problem = problem
+
+    def recover(self, grad, compact_solution) -> np.ndarray:
+        _, v = self.problem.recover(grad, compact_solution, want_field=True)
+        return v
+
+    def average_over_domain(self, velocity: np.ndarray) -> np.ndarray:
+        return velocity.reshape(3, -1).mean(axis=1)
+
+    def average_over_support(self, velocity: np.ndarray) -> np.ndarray:
+        sup = self.problem.support()
+        return velocity.reshape(3, -1)[:, sup].mean(axis=1)
+
+
+class PermeabilityTensor:
+    """src/post/PermeabilityTensor.cpp:11-18: set_column(col, avg_velocity)
+    stores -avg_velocity in column col (row-major k[row*3 + col])."""
+
+    def __init__(self):
+        self.k = np.zeros(9)
+
+    def set_column(self, column: int, avg_velocity):
+        if not 0 <= column < 3:
+            raise IndexError("PermeabilityTensor::set_column index out of range")
+        for row in range(3):
+            self.k[row * 3 + column] = -avg_velocity[row]
+
+    def data(self) -> np.ndarray:
+        return self.k

@@ -1,0 +1,124 @@
+/*
+ * fftperm.h -- C ABI of the GB300 permeability hot path.
+ *
+ * One handle = one periodic voxel grid (nx, ny, nz, voxel size h, viscosity
+ * mu, alias radius p_radius) with all of its state resident on the current
+ * CUDA device.  Host pointers in, host pointers out; status codes instead of
+ * exceptions; no C++ or torch types.  A handle is not thread-safe: use one
+ * handle per host thread (the reference builds one FFT backend + Green
+ * operator per load case, src/app/PermeabilityRunner.cpp:186-203).
+ *
+ * Conventions (the reference's):
+ *   flat index (k*ny + j)*nx + i, x fastest         src/core/Grid3D.hpp:41-43
+ *   fluid mask: nonzero = fluid                      src/geometry/BinaryMedium.cpp:9-11
+ *   full-grid vector fields: x|y|z blocks of N      src/core/Field3D.hpp:16-113
+ *   compact support vectors: v[3*local + comp]      src/bignonnet/TrialForceField.cpp:16-40
+ *   K row-major, K[row*3 + col]                      src/post/PermeabilityTensor.cpp:11-18
+ *
+ * Error behaviour: the reference throws std::invalid_argument on size or
+ * argument errors and std::runtime_error on state errors; here those become
+ * FP_ERR_INVALID and FP_ERR_STATE, and fp_last_error() returns the message.
+ */
+#ifndef FFTPERM_H
+#define FFTPERM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fp_problem* fp_handle;
+
+enum fp_status {
+    FP_OK = 0,
+    FP_ERR_INVALID = 1,     /* invalid argument (reference: std::invalid_argument) */
+    FP_ERR_STATE = 2,       /* call out of order (reference: std::runtime_error)   */
+    FP_ERR_CUDA = 3,        /* CUDA runtime error                                   */
+    FP_ERR_UNSUPPORTED = 4, /* grid edge not a product of 2, 3, 5                   */
+    FP_ERR_NOMEM = 5,       /* device allocation failed                             */
+    FP_ERR_NONFINITE = 6    /* a non-finite value appeared (Brinkman instability)   */
+};
+
+enum fp_precision {
+    FP_PREC_FP64 = 0, /* FFT, Green multiply, scatter/gather in FP64 */
+    FP_PREC_MIXED = 1 /* FFT, Green multiply, scatter/gather in FP32; Lanczos and sums in FP64 */
+};
+
+enum fp_support_mode {
+    FP_SUPPORT_INTERFACE = 0, /* SupportMode::InterfaceOnly, src/core/Types.hpp:25-28 */
+    FP_SUPPORT_FULLSOLID = 1  /* SupportMode::FullSolid */
+};
+
+typedef struct fp_solver_stats {
+    int64_t iterations;        /* SolverResult::iterations        (src/solver/SolverResult.hpp:10-16) */
+    double final_rel_residual; /* SolverResult::final_rel_residual */
+    int32_t converged;         /* SolverResult::converged          */
+    int32_t refinements;       /* mixed precision: outer refinement steps taken */
+    double seconds;            /* wall time of the call            */
+} fp_solver_stats;
+
+/* Replaces the GreenOperator constructor + IFFTBackend::initialize
+ * (src/bignonnet/GreenOperator.cpp:27-52, src/fft/FFTWBackend.cpp:185-299):
+ * plans the FFTs and precomputes the energy-consistent Green tensor. */
+int fp_create(int nx, int ny, int nz, double voxel_size, double mu, int p_radius, int precision,
+              fp_handle* out);
+int fp_destroy(fp_handle h);
+const char* fp_last_error(fp_handle h);
+/* The CUDA stream (cudaStream_t) every call of this handle runs on, so a
+ * caller can time device-pointer calls with events on that stream. */
+void* fp_stream(fp_handle h);
+/* Wait for all work queued on the handle's stream. */
+int fp_synchronize(fp_handle h);
+/* Precision of later applies/solves (FP_PREC_*). */
+int fp_set_precision(fp_handle h, int precision);
+
+/* BinaryMedium + ForceSupport (src/geometry/BinaryMedium.cpp:5-8,
+ * src/bignonnet/ForceSupport.cpp:9-25, src/geometry/InterfaceVoxels.cpp:7-43).
+ * fluid_mask has N bytes.  *nb_out receives N_B (may be NULL). */
+int fp_set_geometry(fp_handle h, const uint8_t* fluid_mask, int support_mode, int64_t* nb_out);
+/* ForceSupport::active_voxels (src/bignonnet/ForceSupport.hpp:22): N_B ascending flat indices. */
+int fp_get_support(fp_handle h, int64_t* out);
+/* Symmetrised Green tensor on the half spectrum, 6 blocks (xx xy xz yy yz zz)
+ * of (nx/2+1)*ny*nz values laid out [kz][ky][kx]: (G(k) + G(-k))/2 with G of
+ * src/bignonnet/GreenOperator.cpp:95-178. */
+int fp_get_green(fp_handle h, double* g6);
+
+/* GreenOperator::apply (src/bignonnet/GreenOperator.cpp:54-65), i.e. the
+ * IFFTBackend forward + spectral Green multiply + inverse chain, on full-grid
+ * SoA fields of 3*N doubles. */
+int fp_green_apply(fp_handle h, const double* force_soa, double* velocity_soa);
+/* BackgroundForce::build (src/bignonnet/BackgroundForce.cpp:14-60), 3*N doubles. */
+int fp_background_force(fp_handle h, const double grad[3], double* f0_soa);
+/* VariationalOperator::apply, the ILinearOperator of the method
+ * (src/bignonnet/VariationalOperator.cpp:19-41): y = A x, 3*N_B doubles. */
+int fp_operator_apply(fp_handle h, const double* x, double* y);
+/* The same with device pointers on the handle's stream (inputs resident in HBM). */
+int fp_operator_apply_device(fp_handle h, const double* d_x, double* d_y);
+/* VariationalRHS::build (src/bignonnet/VariationalRHS.cpp:15-31). */
+int fp_build_rhs(fp_handle h, const double grad[3], double* b);
+/* MinresSolver::solve (src/solver/MinresSolver.cpp:46-218).  x0 may be NULL
+ * (zero start).  hist (may be NULL) receives the residual history, at most
+ * maxit + 1 values; stats->iterations + 1 of them are written. */
+int fp_minres(fp_handle h, const double* b, const double* x0, double tol, int64_t maxit,
+              double* x, double* hist, fp_solver_stats* stats);
+/* VelocityRecovery::recover + average_over_domain
+ * (src/bignonnet/VelocityRecovery.cpp:12-51).  v_soa (3*N, may be NULL)
+ * receives the velocity field, avg its domain average. */
+int fp_recover(fp_handle h, const double grad[3], const double* x, double* v_soa, double avg[3]);
+/* One load case, the body of solve_one_direction
+ * (src/app/PermeabilityRunner.cpp:173-242): RHS, MINRES from x0 (NULL = zero),
+ * recovery, domain-averaged velocity.  x_out (3*N_B, may be NULL) receives the
+ * converged interface forces. */
+int fp_solve_load_case(fp_handle h, const double grad[3], const double* x0, double tol,
+                       int64_t maxit, double avg[3], double* x_out, fp_solver_stats* stats);
+/* Three unit load cases and the K assembly of PermeabilityRunner::run
+ * (src/app/PermeabilityRunner.cpp:700-777): K[row*3+col] = mu <v_row>^(col). */
+int fp_solve_permeability(fp_handle h, double tol, int64_t maxit, double K[9],
+                          fp_solver_stats stats[3]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
