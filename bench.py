@@ -1,0 +1,416 @@
+"""Benchmark: seconds to the permeability tensor of a 256^3 Gaussian-random-field
+cell (correlation length 6 voxels, porosity 0.35, seed 1003), three unit load
+cases, mixed precision (FP32 FFT / Green multiply / scatter-gather, FP64
+Lanczos vectors, inner products and averages), on the GB300.
+
+Output: one JSON line (rank 0).
+
+  value      seconds per permeability tensor, device-resident: the mask and
+             the Green table are on the GPU when the timed region starts;
+             support extraction + 3 x (RHS, MINRES, recovery) + K.  Timed
+             with CUDA events on the library's stream, max over ranks.
+  e2e        the same metric through the C ABI with host buffers: fp_create
+             (FFT plans + Green precompute) + fp_set_geometry (mask H2D) +
+             fp_solve_permeability (K D2H) + fp_destroy, host wall clock.
+  roofline   the operator apply (the five FFT passes of one
+             scatter -> FFT -> Green -> IFFT -> gather), algorithmic bytes per
+             apply / CUDA-event time of the apply, against the measured HBM
+             copy bandwidth.
+  cpu_baseline  the CPU oracle (plain-C restatement of the reference path, FP64,
+             all host threads) on a bounded sample of the same workload,
+             extrapolated to the full solve.
+
+``--impl reference`` times the reference's CPU path the same way (the oracle
+port; the reference's own build cannot travel to the aarch64 GPU host) and
+prints the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "seconds_to_permeability_tensor_256"
+UNIT = "s"
+WORKLOAD = "grf256_phi0.35_l6_seed1003_3loadcases"
+
+# Convergence tolerance of the mixed-precision solve.  The K error against the
+# FP64 solve (tol 1e-10) is measured and reported in every run.
+TOL_MIXED = 1e-7
+TOL_FP64 = 1e-10
+MAXIT = 20000
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(world, v: float) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload_mask(size, seed):
+    from fft_method_test_gb300 import geometry as G
+
+    return G.gaussian_field(size, 6.0, 0.35, seed)
+
+
+# ---------------------------------------------------------------------------
+# clocks sampling (nvidia-smi during the timed region)
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CUDA events on the library's stream
+# ---------------------------------------------------------------------------
+
+class StreamTimer:
+    def __init__(self, stream_ptr):
+        import torch
+
+        self.torch = torch
+        self.stream = torch.cuda.ExternalStream(stream_ptr)
+
+    def event(self):
+        e = self.torch.cuda.Event(enable_timing=True)
+        e.record(self.stream)
+        return e
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_from_profile():
+    """DRAM bytes per operator apply from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "operator_apply_grf256_mixed.md")
+    try:
+        with open(path) as f:
+            for ln in f:
+                if ln.startswith("traffic_bytes_per_apply:"):
+                    return float(ln.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def apply_bytes(nh: int, nb: int, precision: str) -> float:
+    """Algorithmic HBM bytes of one operator apply with the five-pass fused
+    pipeline: 8 sweeps of the 3-component half spectrum, one Green read, the
+    compact input read and output write (FP64 vectors) and the int32 support
+    index read twice."""
+    c = 8 if precision == "mixed" else 16  # complex element
+    g = 4 if precision == "mixed" else 8   # Green element
+    return 8 * 3 * c * nh + 6 * g * nh + 2 * 3 * 8 * nb + 2 * 4 * nb
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (oracle restatement) on a bounded sample
+# ---------------------------------------------------------------------------
+
+def cpu_sample(mask, iterations_full, threads=0, sample_applies=2):
+    """Times the CPU oracle's Green precompute and operator applies at full
+    size and extrapolates to seconds-to-K with the reference's structure:
+    3 x (Green precompute + RHS apply + iterations x apply + recovery apply)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+
+    R = orc.Restatement()
+    t0 = time.perf_counter()
+    ctx = R.context(mask, threads=threads)
+    t_setup = time.perf_counter() - t0  # support + Green precompute
+    x = np.random.default_rng(0).uniform(-1, 1, 3 * ctx.nb)
+    t0 = time.perf_counter()
+    for _ in range(sample_applies):
+        x = ctx.operator_apply(x)
+    t_apply = (time.perf_counter() - t0) / sample_applies
+    ctx.close()
+    cores = threads if threads > 0 else (os.cpu_count() or 1)
+    total = 3 * (t_setup + (iterations_full / 3.0 + 2) * t_apply)
+    return total, cores, dict(setup_s=t_setup, apply_s=t_apply, sample_applies=sample_applies)
+
+
+# ---------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------
+
+def run_ours(args, world, rank, local):
+    import ctypes as C
+
+    import torch
+
+    from fft_method_test_gb300 import _capi
+    from fft_method_test_gb300.permeability import PermeabilityProblem
+
+    torch.cuda.set_device(local)
+    size = args.size
+    mask = workload_mask(size, 1003 + rank)  # weak scaling: one cell per rank
+    lib = _capi.load()
+
+    # setup (untimed): problem with Green table + geometry on the device
+    t0 = time.perf_counter()
+    prob = PermeabilityProblem(mask.shape, precision="mixed")
+    t_create = time.perf_counter() - t0
+    nb = prob.set_geometry(mask)
+    nh = (size // 2 + 1) * size * size
+    timer = StreamTimer(lib.fp_stream(prob.handle))
+
+    # FP64 reference solve on the same cell (plain FP64 GPU MINRES)
+    K64 = None
+    fp64_s = None
+    it64 = None
+    if not args.no_fp64:
+        prob.set_precision("fp64")
+        t0 = time.perf_counter()
+        K64, st64 = prob.solve_permeability(TOL_FP64, MAXIT)
+        fp64_s = time.perf_counter() - t0
+        it64 = [s["iterations"] for s in st64]
+        prob.set_precision("mixed")
+
+    def step():
+        # support extraction on the resident mask + three load cases
+        K, st = prob.solve_permeability(TOL_MIXED, MAXIT)
+        return K, st
+
+    for _ in range(args.warmup):
+        K, st = step()
+    barrier(world)
+    torch.cuda.synchronize()
+    times = []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            e0 = timer.event()
+            K, st = step()
+            e1 = timer.event()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+    torch.cuda.synchronize()
+    barrier(world)
+    t_step = max_over_ranks(world, float(np.mean(times)))
+    its = [s["iterations"] for s in st]
+
+    # roofline: operator applies on device-resident vectors
+    x = torch.randn(3 * nb, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    torch.cuda.synchronize()
+    for _ in range(3):
+        lib.fp_operator_apply_device(prob.handle, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()))
+    reps = 20
+    e0 = timer.event()
+    for _ in range(reps):
+        lib.fp_operator_apply_device(prob.handle, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()))
+    e1 = timer.event()
+    e1.synchronize()
+    t_apply = e0.elapsed_time(e1) / 1e3 / reps
+    peak, peak_kind = measured_peak_hbm()
+    bytes_apply = apply_bytes(nh, nb, "mixed")
+    achieved = bytes_apply / t_apply / 1e9
+
+    # e2e through the C ABI with host buffers
+    mask_c = np.ascontiguousarray(mask, dtype=np.uint8)
+    e2e_times = []
+    for i in range(max(1, args.steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with PermeabilityProblem(mask.shape, precision="mixed") as p2:
+            p2.set_geometry(mask_c)
+            K2, _ = p2.solve_permeability(TOL_MIXED, MAXIT)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e = max_over_ranks(world, float(np.mean(e2e_times)))
+
+    err = None
+    if K64 is not None:
+        err = float(np.linalg.norm(K - K64) / np.linalg.norm(K64))
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        its_full = sum(it64) if it64 else sum(its)
+        total, cores, info = cpu_sample(mask, its_full)
+        cpu = {"value": total, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": "C restatement of the reference path (FP64) at 256^3: support + Green "
+                         "precompute timed once (%.2f s), %d operator applies timed (%.3f s each), "
+                         "extrapolated to 3 x (Green precompute + (%d/3 + 2) applies), the "
+                         "reference's per-load-case structure; MINRES vector work not counted"
+                         % (info["setup_s"], info["sample_applies"], info["apply_s"], its_full)}
+
+    prob.close()
+    if rank != 0:
+        return
+    value = t_step / world if world > 1 else t_step
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "grid": [size, size, size], "load_cases": 3,
+                   "precision": "mixed (fp32 FFT/Green/scatter-gather, fp64 Lanczos)",
+                   "tol": TOL_MIXED, "support_voxels": nb, "iterations": its,
+                   "warm_start": "none", "l2": "working set > L2 (spectral field 3 x (n/2+1) n^2 x 8 B)",
+                   "green_precompute_s": t_create, "parallelism": "replicas" if world > 1 else "1gpu"},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(mask.size),
+                "d2h_bytes_per_step": 72},
+        "K_rel_err_vs_fp64": err, "fp64_seconds": fp64_s, "fp64_iterations": it64,
+        "gpu_launches": None,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic_from_profile(),
+                     "kernel": "operator apply (5 fused FFT passes)", "peak_kind": peak_kind,
+                     "bytes_per_apply": bytes_apply, "apply_ms": t_apply * 1e3},
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_reference(args, world, rank, local):
+    if rank != 0:
+        return
+    size = args.size
+    mask = workload_mask(size, 1003)
+    its_full = int(os.environ.get("FFTPERM_BENCH_ITERS", "0")) or REFERENCE_ITERATIONS_256
+    vals = []
+    for i in range(args.warmup + args.steps):
+        total, cores, info = cpu_sample(mask, its_full, sample_applies=1)
+        if i >= args.warmup:
+            vals.append(total)
+    v = float(np.mean(vals))
+    line = {
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": WORKLOAD, "grid": [size, size, size], "load_cases": 3,
+                   "tol": TOL_FP64},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "C restatement of the reference's CPU path, all host threads: "
+                                   "support + Green precompute and one operator apply timed at "
+                                   "256^3, extrapolated to 3 x (precompute + (%d/3 + 2) applies)"
+                                   % its_full},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# MINRES iterations (sum over the 3 load cases) the FP64 solve of this
+# workload needs at tol 1e-10; used to extrapolate the CPU sample.
+REFERENCE_ITERATIONS_256 = 3000
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank, local)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -31,7 +31,8 @@ FP_SUPPORT_FULLSOLID = 1
 EXPORTED = [
     "fp_create", "fp_destroy", "fp_last_error", "fp_stream", "fp_synchronize",
     "fp_set_precision", "fp_set_geometry",
-    "fp_get_support", "fp_get_green", "fp_green_apply", "fp_background_force",
+    "fp_get_support", "fp_get_green", "fp_fft_forward", "fp_fft_inverse", "fp_green_apply",
+    "fp_background_force",
     "fp_operator_apply", "fp_operator_apply_device", "fp_build_rhs", "fp_minres", "fp_recover",
     "fp_solve_load_case", "fp_solve_permeability",
 ]
@@ -68,6 +69,8 @@ _SIGNATURES = {
     "fp_set_geometry": ([_h, _u8p, C.c_int, C.POINTER(C.c_int64)], C.c_int),
     "fp_get_support": ([_h, _i64p], C.c_int),
     "fp_get_green": ([_h, _dp], C.c_int),
+    "fp_fft_forward": ([_h, _dp, _dp], C.c_int),
+    "fp_fft_inverse": ([_h, _dp, _dp], C.c_int),
     "fp_green_apply": ([_h, _dp, _dp], C.c_int),
     "fp_background_force": ([_h, _dp, _dp], C.c_int),
     "fp_operator_apply": ([_h, _dp, _dp], C.c_int),

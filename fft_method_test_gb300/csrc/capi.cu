@@ -380,6 +380,50 @@ int fp_green_apply(fp_handle h, const double* force_soa, double* velocity_soa) {
     return FP_OK;
 }
 
+int fp_fft_forward(fp_handle h, const double* real_soa, double* half_spectrum) {
+    if (!h || !real_soa || !half_spectrum) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    int rc = alloc_dense(P);
+    if (rc) return rc;
+    FP_CUDA(cudaMemcpyAsync(P.d_dense_in, real_soa, sizeof(double) * 3 * (size_t)P.n,
+                            cudaMemcpyHostToDevice, P.stream),
+            "copy");
+    fp::ApplyArgs a;
+    a.src = P.d_dense_in;
+    a.src_kind = fp::kSrcDense;
+    a.stage = fp::kStageForward;
+    a.precision = fp::kFP64;
+    int nparts = 0;
+    FP_CUDA(fp::launch_apply(P, a, &nparts), "forward fft");
+    FP_CUDA(cudaMemcpyAsync(half_spectrum, P.d_spec, sizeof(double2) * 3 * (size_t)P.nh,
+                            cudaMemcpyDeviceToHost, P.stream),
+            "copy");
+    FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+    return FP_OK;
+}
+
+int fp_fft_inverse(fp_handle h, const double* half_spectrum, double* real_soa) {
+    if (!h || !real_soa || !half_spectrum) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    int rc = alloc_dense(P);
+    if (rc) return rc;
+    FP_CUDA(cudaMemcpyAsync(P.d_spec, half_spectrum, sizeof(double2) * 3 * (size_t)P.nh,
+                            cudaMemcpyHostToDevice, P.stream),
+            "copy");
+    fp::ApplyArgs a;
+    a.dst = P.d_dense_out;
+    a.dst_kind = fp::kDstDense;
+    a.stage = fp::kStageInverse;
+    a.precision = fp::kFP64;
+    int nparts = 0;
+    FP_CUDA(fp::launch_apply(P, a, &nparts), "inverse fft");
+    FP_CUDA(cudaMemcpyAsync(real_soa, P.d_dense_out, sizeof(double) * 3 * (size_t)P.n,
+                            cudaMemcpyDeviceToHost, P.stream),
+            "copy");
+    FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+    return FP_OK;
+}
+
 int fp_background_force(fp_handle h, const double grad[3], double* f0_soa) {
     if (!h || !grad || !f0_soa) return FP_ERR_INVALID;
     Problem& P = h->P;

@@ -122,6 +122,13 @@ enum XDest {
     kDstDense = 1     // dense SoA field (3 x n) + partial sums over all voxels
 };
 
+// Which part of the pipeline launch_apply runs.
+enum Stage {
+    kStageFull = 0,     // forward x, y, z + Green + inverse z, y, x
+    kStageForward = 1,  // forward x, y, z only: the half spectrum is left in d_spec
+    kStageInverse = 2   // inverse z, y, x of the half spectrum in d_spec
+};
+
 struct ApplyArgs {
     const double* src = nullptr;     // compact or dense source
     const double* src_sum = nullptr; // device: component sums of the compact source (3), or null
@@ -133,6 +140,7 @@ struct ApplyArgs {
     int dst_kind = kDstCompact;
     const int* skip = nullptr;       // device flag: when nonzero every pass returns at once
     int precision = -1;              // kFP64 / kMixed; -1 = the problem's default
+    int stage = kStageFull;
 };
 
 // Runs the five passes (forward x, y, z + Green + inverse z, inverse y,

@@ -290,7 +290,9 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 256 : 512) k_ypass(YArgs a) {
 // P3: z forward, Green multiply, z inverse (one ky, a tile of kx, 3 comps)
 // ---------------------------------------------------------------------------
 
-template <typename T>
+// ZMODE: 0 = forward z, Green multiply, inverse z; 1 = forward z only;
+// 2 = inverse z only
+template <typename T, int ZMODE>
 __global__ void __launch_bounds__(sizeof(T) == 8 ? 256 : 512) k_zgreen(ZArgs a) {
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
@@ -316,10 +318,10 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 256 : 512) k_zgreen(ZArgs a) 
     const int q = threadIdx.x / tpl;
     const int lane = threadIdx.x - q * tpl;
     T2* my = q < 3 * tz ? lines + q * nz : (T2*)nullptr;
-    fft_line<-1>(my, a.plan, lane);
+    if (ZMODE != 2) fft_line<-1>(my, a.plan, lane);
     // Green multiply: u = G f at every (kz, kx)
     const T* g = reinterpret_cast<const T*>(a.green);
-    for (int t = threadIdx.x; t < nz * tz; t += blockDim.x) {
+    for (int t = threadIdx.x; ZMODE == 0 && t < nz * tz; t += blockDim.x) {
         const int c = t % tz;
         const int z = t / tz;
         const long long gi = z * plane + off0 + c;
@@ -334,7 +336,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 256 : 512) k_zgreen(ZArgs a) 
         *fz = cmk<T2>(gxz * ax.x + gyz * ay.x + gzz * az.x, gxz * ax.y + gyz * ay.y + gzz * az.y);
     }
     __syncthreads();
-    fft_line<+1>(my, a.plan, lane);
+    if (ZMODE != 1) fft_line<+1>(my, a.plan, lane);
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
         const int c = t % tz;
         const int rest = t / tz;
@@ -497,7 +499,7 @@ static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     const size_t xsmem = (size_t)nq * P.nx * elem;
     const int xblocks = (int)((P.nrows + x.rows_per_cta - 1) / x.rows_per_cta);
 
-    switch (aa.src_kind) {
+    if (aa.stage != kStageInverse) switch (aa.src_kind) {
         case kSrcCompact:
             cudaFuncSetAttribute(k_xfwd<T, kSrcCompact>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xsmem);
             k_xfwd<T, kSrcCompact><<<xblocks, xthreads, xsmem, P.stream>>>(x);
@@ -534,7 +536,7 @@ static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     dim3 ygrid((P.nxh + y.tx - 1) / y.tx, P.nz, 3);
     cudaFuncSetAttribute(k_ypass<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ysmem);
     cudaFuncSetAttribute(k_ypass<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ysmem);
-    if (P.ny > 1) k_ypass<T, -1><<<ygrid, ythreads, ysmem, P.stream>>>(y);
+    if (P.ny > 1 && aa.stage != kStageInverse) k_ypass<T, -1><<<ygrid, ythreads, ysmem, P.stream>>>(y);
 
     // z pass with the Green multiply
     ZArgs z{};
@@ -554,8 +556,19 @@ static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     const int zthreads = std::max(32, ((3 * z.tz * P.pz.dev.tpl + 31) / 32) * 32);
     const size_t zsmem = (size_t)3 * z.tz * P.nz * elem;
     dim3 zgrid((P.nxh + z.tz - 1) / z.tz, P.ny);
-    cudaFuncSetAttribute(k_zgreen<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zsmem);
-    k_zgreen<T><<<zgrid, zthreads, zsmem, P.stream>>>(z);
+    if (aa.stage != kStageInverse) {
+        if (aa.stage == kStageForward) {
+            cudaFuncSetAttribute(k_zgreen<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zsmem);
+            k_zgreen<T, 1><<<zgrid, zthreads, zsmem, P.stream>>>(z);
+            *nparts = 0;
+            return cudaGetLastError();
+        }
+        cudaFuncSetAttribute(k_zgreen<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zsmem);
+        k_zgreen<T, 0><<<zgrid, zthreads, zsmem, P.stream>>>(z);
+    } else {
+        cudaFuncSetAttribute(k_zgreen<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zsmem);
+        k_zgreen<T, 2><<<zgrid, zthreads, zsmem, P.stream>>>(z);
+    }
 
     if (P.ny > 1) k_ypass<T, +1><<<ygrid, ythreads, ysmem, P.stream>>>(y);
 

@@ -129,6 +129,26 @@ class PermeabilityProblem:
         self._check(self.lib.fp_green_apply(self._h, f.ravel(), u))
         return u.reshape((3,) + self.shape)
 
+    def fft_forward(self, real_field: np.ndarray) -> np.ndarray:
+        """Half spectrum (3, nz, ny, nx//2+1) complex of a real (3, nz, ny, nx) field."""
+        f = np.ascontiguousarray(real_field, dtype=np.float64)
+        if f.size != 3 * self.n:
+            raise ValueError("FFT backend forward grid size mismatch")
+        nz, ny, nx = self.shape
+        out = np.zeros(3 * nz * ny * (nx // 2 + 1) * 2)
+        self._check(self.lib.fp_fft_forward(self._h, f.ravel(), out))
+        return out.view(np.complex128).reshape(3, nz, ny, nx // 2 + 1)
+
+    def fft_inverse(self, half_spectrum: np.ndarray) -> np.ndarray:
+        """Real part of the inverse DFT (times 1/N) of a Hermitian half spectrum."""
+        nz, ny, nx = self.shape
+        h = np.ascontiguousarray(half_spectrum, dtype=np.complex128)
+        if h.shape != (3, nz, ny, nx // 2 + 1):
+            raise ValueError("FFT backend inverse grid size mismatch")
+        out = np.zeros(3 * self.n)
+        self._check(self.lib.fp_fft_inverse(self._h, h.view(np.float64).ravel(), out))
+        return out.reshape((3,) + self.shape)
+
     def background_force(self, grad) -> np.ndarray:
         f0 = np.zeros(3 * self.n)
         self._check(self.lib.fp_background_force(self._h, np.asarray(grad, np.float64), f0))

@@ -84,6 +84,17 @@ int fp_get_support(fp_handle h, int64_t* out);
  * src/bignonnet/GreenOperator.cpp:95-178. */
 int fp_get_green(fp_handle h, double* g6);
 
+/* IFFTBackend::forward (src/fft/IFFTBackend.hpp:18-19, FFTWBackend.cpp:301-362)
+ * in R2C form: the unnormalised forward 3-D DFT of each component of a real
+ * SoA field (3*N doubles), returned as the half spectrum kx in [0, nx/2]:
+ * 3 blocks of (nx/2+1)*ny*nz interleaved (re, im) doubles laid out
+ * [kz][ky][kx].  The other half is the complex conjugate (real input). */
+int fp_fft_forward(fp_handle h, const double* real_soa, double* half_spectrum);
+/* IFFTBackend::inverse (src/fft/IFFTBackend.hpp:21-22, FFTWBackend.cpp:364-420)
+ * in C2R form: real part of the inverse DFT times 1/N.  The input half
+ * spectrum stands for the Hermitian part (X(k) + conj X(-k))/2 of a full
+ * spectrum X, whose inverse has exactly the real part the reference keeps. */
+int fp_fft_inverse(fp_handle h, const double* half_spectrum, double* real_soa);
 /* GreenOperator::apply (src/bignonnet/GreenOperator.cpp:54-65), i.e. the
  * IFFTBackend forward + spectral Green multiply + inverse chain, on full-grid
  * SoA fields of 3*N doubles. */

@@ -1,0 +1,42 @@
+"""The C ABI library builds, loads and exports every symbol of include/fftperm.h.
+No compute call is made (no GPU needed)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def declared_symbols():
+    with open(os.path.join(ROOT, "include", "fftperm.h")) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(fp_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    from fft_method_test_gb300 import _capi, build
+
+    path = build.build()
+    lib = C.CDLL(path)
+    syms = declared_symbols()
+    assert len(syms) >= 18
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert set(syms) == set(_capi.EXPORTED)
+
+
+def test_python_mirror_loads_and_validates_without_gpu():
+    from fft_method_test_gb300 import _capi
+    from fft_method_test_gb300.permeability import MinresSolver, PermeabilityTensor
+
+    _capi.load()
+    with pytest.raises(ValueError):
+        MinresSolver(0.0, 10)
+    t = PermeabilityTensor()
+    t.set_column(1, [1.0, 2.0, 3.0])
+    assert list(t.data()[[1, 4, 7]]) == [-1.0, -2.0, -3.0]
+    with pytest.raises(IndexError):
+        t.set_column(3, [0, 0, 0])
