@@ -60,6 +60,10 @@ def parse():
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--mode", default="solve", choices=["solve", "apply"],
+                    help="apply: only run --reps operator applies per precision (for profilers)")
+    ap.add_argument("--precision", default="mixed,fp64", help="precisions for --mode apply")
+    ap.add_argument("--reps", type=int, default=3)
     return ap.parse_args()
 
 
@@ -399,8 +403,33 @@ def run_reference(args, world, rank, local):
 REFERENCE_ITERATIONS_256 = 3000
 
 
+def run_applies(args):
+    """Profiling entry: operator applies on device-resident vectors, nothing else."""
+    import ctypes as C
+
+    import torch
+
+    from fft_method_test_gb300.permeability import PermeabilityProblem
+
+    mask = workload_mask(args.size, 1003)
+    for prec in args.precision.split(","):
+        with PermeabilityProblem(mask.shape, precision=prec) as p:
+            nb = p.set_geometry(mask)
+            x = torch.randn(3 * nb, dtype=torch.float64, device="cuda")
+            y = torch.empty_like(x)
+            torch.cuda.synchronize()
+            for _ in range(args.reps):
+                p.lib.fp_operator_apply_device(p.handle, C.c_void_p(x.data_ptr()),
+                                               C.c_void_p(y.data_ptr()))
+            p.lib.fp_synchronize(p.handle)
+    print("applies done", flush=True)
+
+
 def main():
     args = parse()
+    if args.mode == "apply":
+        run_applies(args)
+        return
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank, local)

@@ -34,7 +34,8 @@ EXPORTED = [
     "fp_get_support", "fp_get_green", "fp_fft_forward", "fp_fft_inverse", "fp_green_apply",
     "fp_background_force",
     "fp_operator_apply", "fp_operator_apply_device", "fp_build_rhs", "fp_minres", "fp_recover",
-    "fp_solve_load_case", "fp_solve_permeability",
+    "fp_solve_load_case", "fp_solve_permeability", "fp_brinkman_solve",
+    "fp_brinkman_permeability", "fp_brinkman_last_error",
 ]
 
 
@@ -53,7 +54,24 @@ class SolverStats(C.Structure):
                     seconds=float(self.seconds))
 
 
+class BrinkmanStats(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_int32),
+        ("converged", C.c_int32),
+        ("residual", C.c_double),
+        ("porosity", C.c_double),
+        ("viscosity", C.c_double),
+        ("seconds", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return dict(iterations=int(self.iterations), converged=bool(self.converged),
+                    residual=float(self.residual), porosity=float(self.porosity),
+                    viscosity=float(self.viscosity), seconds=float(self.seconds))
+
+
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
 _u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 _i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
 _h = C.c_void_p
@@ -82,6 +100,13 @@ _SIGNATURES = {
     "fp_solve_load_case": ([_h, _dp, C.c_void_p, C.c_double, C.c_int64, _dp, C.c_void_p,
                             C.POINTER(SolverStats)], C.c_int),
     "fp_solve_permeability": ([_h, C.c_double, C.c_int64, _dp, C.POINTER(SolverStats)], C.c_int),
+    "fp_brinkman_solve": ([C.c_int, C.c_int, C.c_int, _u32p, C.c_uint32, C.c_double, C.c_double,
+                           C.c_double, C.c_double, C.c_int, _dp, C.c_void_p, C.c_void_p,
+                           C.c_void_p, C.c_void_p, _dp, C.POINTER(BrinkmanStats)], C.c_int),
+    "fp_brinkman_permeability": ([C.c_int, C.c_int, C.c_int, _u32p, C.c_uint32, C.c_double,
+                                  C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
+                                  C.c_double, _dp, C.POINTER(BrinkmanStats)], C.c_int),
+    "fp_brinkman_last_error": ([], C.c_char_p),
 }
 
 _lib = None

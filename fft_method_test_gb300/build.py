@@ -18,6 +18,9 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libfftperm.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
+# Files whose arithmetic must round exactly like the reference's (no FMA
+# contraction): the Brinkman stencils reproduce the reference field values.
+NO_FMA = {"kernels_brinkman.cu"}
 
 
 def _nvcc() -> str:
@@ -51,7 +54,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
         o = os.path.join(BUILD, os.path.basename(s)[:-3] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, "-c", s, "-o", o])
+            extra = ["-fmad=false"] if os.path.basename(s) in NO_FMA else []
+            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, *extra, "-c", s, "-o", o])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

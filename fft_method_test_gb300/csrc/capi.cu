@@ -9,6 +9,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -78,14 +79,14 @@ int alloc_dense(Problem& P) {
 int ensure_green32(Problem& P) {
     if (P.d_green32) return FP_OK;
     FP_CUDA(dalloc(&P.d_green32, 6 * (size_t)P.nh), "cudaMalloc green32");
-    // convert from the FP64 table
-    std::vector<double> h(6 * (size_t)P.nh);
-    FP_CUDA(cudaMemcpy(h.data(), P.d_green64, sizeof(double) * h.size(), cudaMemcpyDeviceToHost),
-            "green copy");
-    std::vector<float> f(h.size());
-    for (size_t i = 0; i < h.size(); ++i) f[i] = (float)h[i];
-    FP_CUDA(cudaMemcpy(P.d_green32, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice),
-            "green copy");
+    FP_CUDA(fp::launch_green(P, nullptr, P.d_green32), "green precompute");
+    return FP_OK;
+}
+
+int ensure_green64(Problem& P) {
+    if (P.d_green64) return FP_OK;
+    FP_CUDA(dalloc(&P.d_green64, 6 * (size_t)P.nh), "cudaMalloc green64");
+    FP_CUDA(fp::launch_green(P, P.d_green64, nullptr), "green precompute");
     return FP_OK;
 }
 
@@ -242,12 +243,12 @@ int fp_create(int nx, int ny, int nz, double voxel_size, double mu, int p_radius
     FP_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
     FP_CUDA(cudaDeviceGetAttribute(&P.sm_count, cudaDevAttrMultiProcessorCount, dev), "attr");
     FP_CUDA(cudaStreamCreateWithFlags(&P.stream, cudaStreamNonBlocking), "stream");
+    if (const char* t = std::getenv("FFTPERM_TILE_YZ")) P.tile_yz = std::atoi(t);
     std::string err;
     if (!fp::make_axis_plan(nx, P.px, err) || !fp::make_axis_plan(ny, P.py, err) ||
         !fp::make_axis_plan(nz, P.pz, err))
         return fail(P, FP_ERR_UNSUPPORTED, err);
     FP_CUDA(dalloc(reinterpret_cast<double2**>(&P.d_spec), 3 * (size_t)P.nh), "cudaMalloc spec");
-    FP_CUDA(dalloc(&P.d_green64, 6 * (size_t)P.nh), "cudaMalloc green");
     const size_t nparts = (size_t)std::max<long long>(fp::kMaxPartials, P.nrows + 64);
     FP_CUDA(dalloc(&P.d_partials, 4 * nparts), "cudaMalloc partials");
     FP_CUDA(dalloc(&P.d_red, 64), "cudaMalloc red");
@@ -256,11 +257,8 @@ int fp_create(int nx, int ny, int nz, double voxel_size, double mu, int p_radius
     FP_CUDA(dalloc(&P.d_row_ptr, (size_t)P.nrows + 1), "cudaMalloc row_ptr");
     FP_CUDA(dalloc(&P.d_row_cnt, (size_t)P.nrows + 1), "cudaMalloc row_cnt");
     FP_CUDA(dalloc(&P.d_mask, (size_t)P.n), "cudaMalloc mask");
-    FP_CUDA(fp::launch_green(P), "green precompute");
-    if (precision == FP_PREC_MIXED) {
-        int rc = ensure_green32(P);
-        if (rc) return rc;
-    }
+    int rc = (precision == FP_PREC_MIXED) ? ensure_green32(P) : ensure_green64(P);
+    if (rc) return rc;
     return FP_OK;
 }
 
@@ -306,10 +304,8 @@ int fp_set_precision(fp_handle h, int precision) {
     Problem& P = h->P;
     if (precision != FP_PREC_FP64 && precision != FP_PREC_MIXED)
         return fail(P, FP_ERR_INVALID, "unknown precision mode");
-    if (precision == FP_PREC_MIXED) {
-        int rc = ensure_green32(P);
-        if (rc) return rc;
-    }
+    int rc = (precision == FP_PREC_MIXED) ? ensure_green32(P) : ensure_green64(P);
+    if (rc) return rc;
     P.precision = precision;
     return FP_OK;
 }
@@ -353,6 +349,8 @@ int fp_get_support(fp_handle h, int64_t* out) {
 int fp_get_green(fp_handle h, double* g6) {
     if (!h || !g6) return FP_ERR_INVALID;
     Problem& P = h->P;
+    int rc = ensure_green64(P);
+    if (rc) return rc;
     FP_CUDA(cudaMemcpy(g6, P.d_green64, sizeof(double) * 6 * (size_t)P.nh, cudaMemcpyDeviceToHost),
             "copy");
     return FP_OK;

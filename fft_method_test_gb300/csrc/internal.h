@@ -58,6 +58,7 @@ struct Problem {
     int precision = kFP64;
     cudaStream_t stream = nullptr;
     int sm_count = 0;
+    int tile_yz = 0;  // kx columns per CTA of the y and z passes (0 = default)
 
     AxisPlan px, py, pz;
 
@@ -106,7 +107,8 @@ constexpr int kMaxPartials = 8192;
 
 // ---- setup kernels (kernels_setup.cu) ----
 cudaError_t launch_support(Problem& P);
-cudaError_t launch_green(Problem& P);
+// Computes the Green table into g64 and/or g32 (either may be null).
+cudaError_t launch_green(Problem& P, double* g64, float* g32);
 
 // ---- operator passes (kernels_fft.cu) ----
 // Source of the forward x pass.

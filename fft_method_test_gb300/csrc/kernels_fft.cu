@@ -60,19 +60,24 @@ bool make_axis_plan(int n, AxisPlan& p, std::string& err) {
     p = AxisPlan{};
     if (n > 640) {
         // the FP64 z pass keeps the three components of one column in one
-        // CTA of at most 256 threads: 3 * ceil(n/8) <= 256
+        // CTA of at most 256 threads
         err = "grid edge " + std::to_string(n) + " exceeds the supported maximum of 640";
         return false;
     }
     p.dev.n = n;
-    p.dev.tpl = std::max(1, (n + 7) / 8);
-    const int ns = factor_radices(n, p.dev.radix, 4);
-    p.dev.nstage64 = factor_radices(n, p.dev.radix64, 3);
-    if (ns < 0) {
+    const int ns32 = factor_radices(n, p.dev.radix32, 4);
+    const int ns64 = factor_radices(n, p.dev.radix64, 3);
+    if (ns32 < 0 || ns64 < 0) {
         err = "grid edge " + std::to_string(n) + " is not a product of 2, 3 and 5";
         return false;
     }
-    p.dev.nstage = ns;
+    p.dev.nstage32 = ns32;
+    p.dev.nstage64 = ns64;
+    int r32 = 1, r64 = 1;
+    for (int i = 0; i < ns32; ++i) r32 = std::max(r32, p.dev.radix32[i]);
+    for (int i = 0; i < ns64; ++i) r64 = std::max(r64, p.dev.radix64[i]);
+    p.dev.tpl32 = (n + r32 - 1) / r32;
+    p.dev.tpl64 = (n + r64 - 1) / r64;
     std::vector<double2> h64(n);
     std::vector<float2> h32(n);
     const double two_pi = 6.283185307179586476925286766559;
@@ -106,6 +111,8 @@ void free_axis_plan(AxisPlan& p) {
 
 struct XArgs {
     int nx, ny, nz, nxh;
+    int ld;        // padded shared-memory line stride
+    long long rs;  // row stride of the spectral field (complex elements)
     long long n, nh, nrows;
     int rows_per_cta;
     FftPlanDev plan;
@@ -126,16 +133,16 @@ struct XArgs {
 };
 
 struct YArgs {
-    int ny, nxh, tx;
-    long long nh;
+    int ny, nxh, tx, ld;
+    long long nh, rs;
     FftPlanDev plan;
     void* spec;
     const int* skip;
 };
 
 struct ZArgs {
-    int ny, nz, nxh, tz;
-    long long nh;
+    int ny, nz, nxh, tz, ld;
+    long long nh, rs, plane, gstride;
     FftPlanDev plan;
     const void* green;
     void* spec;
@@ -147,12 +154,13 @@ struct ZArgs {
 // ---------------------------------------------------------------------------
 
 template <typename T, int SRC>
-__global__ void __launch_bounds__(sizeof(T) == 8 ? 256 : 512) k_xfwd(XArgs a) {
+__global__ void __launch_bounds__(256, 3) k_xfwd(XArgs a) {
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T2* lines = reinterpret_cast<T2*>(smem_raw);
     const int nx = a.nx;
+    const int ld = a.ld;
     const long long r0 = (long long)blockIdx.x * a.rows_per_cta;
     const int rows = (int)min((long long)a.rows_per_cta, a.nrows - r0);
     const int nreal = 3 * rows;
@@ -184,7 +192,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 256 : 512) k_xfwd(XArgs a) {
                 }
             }
         }
-        lines[t] = cmk<T2>(vr, vi);
+        lines[q * ld + pidx<T2>(x)] = cmk<T2>(vr, vi);
     }
     __syncthreads();
 
@@ -199,29 +207,51 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 256 : 512) k_xfwd(XArgs a) {
         }
         const int s0 = a.row_ptr[r0];
         const int s1 = a.row_ptr[r0 + rows];
-        for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
-            const long long idx = a.support[s];
-            const int rl = (int)(idx / nx - r0);
-            const int x = (int)(idx - (r0 + rl) * nx);
+        constexpr int U = 4;  // support entries in flight per thread
+        for (int sb = s0 + threadIdx.x; sb < s1; sb += U * blockDim.x) {
+            int sidx[U];
+            double cv[U][3];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                double val = 0.0;
-                if (SRC != kSrcF0) val = a.src[3LL * s + c] - mean[c];
-                if (SRC != kSrcCompact) val += a.f0_support[c];
-                const int L = 3 * rl + c;
-                T2* p = &lines[(L >> 1) * nx + x];
-                if (L & 1) p->y = (T)val; else p->x = (T)val;
+            for (int u = 0; u < U; ++u) {
+                const int s = sb + u * blockDim.x;
+                sidx[u] = -1;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) cv[u][c] = 0.0;
+                if (s < s1) {
+                    sidx[u] = a.support[s];
+                    if (SRC != kSrcF0)
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) cv[u][c] = a.src[3LL * s + c];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (sidx[u] < 0) continue;
+                const long long idx = sidx[u];
+                const int rl = (int)(idx / nx - r0);
+                const int x = (int)(idx - (r0 + rl) * nx);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    double val = 0.0;
+                    if (SRC != kSrcF0) val = cv[u][c] - mean[c];
+                    if (SRC != kSrcCompact) val += a.f0_support[c];
+                    const int L = 3 * rl + c;
+                    T2* p = &lines[(L >> 1) * ld + pidx<T2>(x)];
+                    if (L & 1) p->y = (T)val; else p->x = (T)val;
+                }
             }
         }
         __syncthreads();
     }
 
-    // 3) forward FFT of every complex line
+    // 3) forward FFT of every complex line (shared memory in and out)
     {
-        const int tpl = a.plan.tpl;
+        const int tpl = plan_tpl<T2>(a.plan);
         const int q = threadIdx.x / tpl;
         const int lane = threadIdx.x - q * tpl;
-        fft_line<-1>(q < nq ? lines + q * nx : (T2*)nullptr, a.plan, lane);
+        T2* my = lines + (q < nq ? q : 0) * ld;
+        fft_lines<-1, kIoSmem, kIoSmem, 1>(&my, a.plan, lane, q < nq, false, NoSrc<T2>{},
+                                            NoDst<T2>{});
     }
 
     // 4) separate the two real spectra and store the half spectrum
@@ -230,119 +260,205 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 256 : 512) k_xfwd(XArgs a) {
     for (int t = threadIdx.x; t < tot2; t += blockDim.x) {
         const int q = t / nxh;
         const int k = t - q * nxh;
-        const T2 zk = lines[q * nx + k];
+        const T2 zk = lines[q * ld + pidx<T2>(k)];
         const int kn = (k == 0) ? 0 : nx - k;
-        const T2 zn = lines[q * nx + kn];
+        const T2 zn = lines[q * ld + pidx<T2>(kn)];
         const T2 A = cmk<T2>((T)0.5 * (zk.x + zn.x), (T)0.5 * (zk.y - zn.y));
         const T2 B = cmk<T2>((T)0.5 * (zk.y + zn.y), (T)0.5 * (zn.x - zk.x));
         {
             const int L = 2 * q;
             const int rl = L / 3;
             const int c = L - 3 * rl;
-            spec[c * a.nh + (r0 + rl) * nxh + k] = A;
+            spec[c * a.nh + (r0 + rl) * a.rs + k] = A;
         }
         const int L = 2 * q + 1;
         if (L < nreal) {
             const int rl = L / 3;
             const int c = L - 3 * rl;
-            spec[c * a.nh + (r0 + rl) * nxh + k] = B;
+            spec[c * a.nh + (r0 + rl) * a.rs + k] = B;
         }
     }
 }
 
 // ---------------------------------------------------------------------------
-// P2 / P4: y pass (one z plane, a tile of kx columns, one component)
+// P2 / P4: y pass (one z plane, a tile of kx columns, all three components
+// per thread; the first stage reads HBM, the last stage writes HBM)
 // ---------------------------------------------------------------------------
 
+template <typename T2>
+struct ColIo {
+    T2* base;          // element (comp 0, y 0) of this thread's column
+    long long cstride; // component block stride
+    long long estride; // stride between successive elements of the line
+    __device__ __forceinline__ T2 operator()(int l, int i) const {
+        return base[l * cstride + (long long)i * estride];
+    }
+    __device__ __forceinline__ void operator()(int l, int i, T2 v) const {
+        base[l * cstride + (long long)i * estride] = v;
+    }
+};
+
 template <typename T, int S>
-__global__ void __launch_bounds__(sizeof(T) == 8 ? 256 : 512) k_ypass(YArgs a) {
+__global__ void __launch_bounds__(256) k_ypass(YArgs a) {
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T2* lines = reinterpret_cast<T2*>(smem_raw);
-    const int ny = a.ny;
-    const int k0 = blockIdx.x * a.tx;
-    const int tx = min(a.tx, a.nxh - k0);
+    const int tx = a.tx;
+    const int k0 = blockIdx.x * tx;
+    const int c = threadIdx.x % tx;
+    const int lane = threadIdx.x / tx;
+    const bool active = (k0 + c) < a.nxh;
     const long long z = blockIdx.y;
-    const int comp = blockIdx.z;
-    T2* base = reinterpret_cast<T2*>(a.spec) + comp * a.nh + z * (long long)ny * a.nxh + k0;
-    const int total = ny * tx;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int y = t / tx;
-        const int c = t - y * tx;
-        lines[c * ny + y] = base[(long long)y * a.nxh + c];
-    }
-    __syncthreads();
-    {
-        const int tpl = a.plan.tpl;
-        const int q = threadIdx.x / tpl;
-        const int lane = threadIdx.x - q * tpl;
-        fft_line<S>(q < tx ? lines + q * ny : (T2*)nullptr, a.plan, lane);
-    }
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int y = t / tx;
-        const int c = t - y * tx;
-        base[(long long)y * a.nxh + c] = lines[c * ny + y];
-    }
+    ColIo<T2> io;
+    io.base = reinterpret_cast<T2*>(a.spec) + z * (long long)a.ny * a.rs + k0 + (active ? c : 0);
+    io.cstride = a.nh;
+    io.estride = a.rs;
+    T2* sl[3];
+#pragma unroll
+    for (int l = 0; l < 3; ++l) sl[l] = lines + (l * tx + c) * a.ld;
+    fft_lines<S, kIoFunc, kIoFunc, 3>(sl, a.plan, lane, active, S > 0, io, io);
 }
 
 // ---------------------------------------------------------------------------
-// P3: z forward, Green multiply, z inverse (one ky, a tile of kx, 3 comps)
+// P3: z forward, Green multiply in registers, z inverse (one ky, a tile of
+// kx columns, three components per thread).  The inverse runs the radices in
+// reverse order, so its first stage consumes exactly the elements the
+// forward's last stage left in this thread's registers.
 // ---------------------------------------------------------------------------
+
+template <int RL, typename T>
+__device__ __forceinline__ void z_fused(const ZArgs& a, c_t<T>* const* sl, ColIo<c_t<T>>& io,
+                                        int c, int lane, bool active) {
+    using T2 = c_t<T>;
+    const FftPlanDev& p = a.plan;
+    const T2* tw = plan_tw<T2>(p);
+    const int nst = plan_nstage<T2>(p);
+    const int tpl = plan_tpl<T2>(p);
+    const int n = p.n;
+    NoSrc<T2> nsrc;
+    NoDst<T2> ndst;
+    // forward stages but the last
+    int ns = 1;
+    for (int s = 0; s < nst - 1; ++s) {
+        const int R = plan_radix<T2>(p, s);
+        if (s == 0)
+            fft_stage_rt<-1, kIoFunc, kIoSmem, 3>(R, sl, n, ns, lane, tpl, active, tw, io, ndst);
+        else
+            fft_stage_rt<-1, kIoSmem, kIoSmem, 3>(R, sl, n, ns, lane, tpl, active, tw, nsrc, ndst);
+        ns *= R;
+    }
+    // last forward stage into registers
+    constexpr int KM = StageRegs<T2, RL>::KM;
+    T2 v[3][KM][RL];
+    zero_regs(v);
+    if (nst == 1)
+        stage_load<RL, kIoFunc, 3>(v, sl, n, lane, tpl, active, io);
+    else
+        stage_load<RL, kIoSmem, 3>(v, sl, n, lane, tpl, active, nsrc);
+    stage_compute<RL, -1, 3>(v, n, ns, lane, tpl, active, tw);
+    // Green multiply: output r of butterfly j is kz = j + r * (n / RL)
+    const int m = n / RL;
+    if (active) {
+        const T* g = reinterpret_cast<const T*>(a.green);
+        const long long gb = (long long)blockIdx.y * a.rs + blockIdx.x * a.tz + c;
+#pragma unroll
+        for (int kk = 0; kk < KM; ++kk) {
+            const int j = lane + kk * tpl;
+            if (j < m) {
+#pragma unroll
+                for (int r = 0; r < RL; ++r) {
+                    const long long gi = (long long)(j + r * m) * a.plane + gb;
+                    const T gxx = g[gi], gxy = g[a.gstride + gi], gxz = g[2 * a.gstride + gi];
+                    const T gyy = g[3 * a.gstride + gi], gyz = g[4 * a.gstride + gi];
+                    const T gzz = g[5 * a.gstride + gi];
+                    const int o = out_slot<RL>(r);
+                    const T2 ax = v[0][kk][o], ay = v[1][kk][o], az = v[2][kk][o];
+                    v[0][kk][o] = cmk<T2>(gxx * ax.x + gxy * ay.x + gxz * az.x, gxx * ax.y + gxy * ay.y + gxz * az.y);
+                    v[1][kk][o] = cmk<T2>(gxy * ax.x + gyy * ay.x + gyz * az.x, gxy * ax.y + gyy * ay.y + gyz * az.y);
+                    v[2][kk][o] = cmk<T2>(gxz * ax.x + gyz * ay.x + gzz * az.x, gxz * ax.y + gyz * ay.y + gzz * az.y);
+                }
+            }
+        }
+    }
+    // first inverse stage (radix RL, Ns = 1: no twiddles) on the same registers
+    T2 u[3][KM][RL];
+    zero_regs(u);
+#pragma unroll
+    for (int l = 0; l < 3; ++l)
+#pragma unroll
+        for (int kk = 0; kk < KM; ++kk)
+#pragma unroll
+            for (int r = 0; r < RL; ++r) u[l][kk][r] = v[l][kk][out_slot<RL>(r)];
+    stage_compute<RL, +1, 3>(u, n, 1, lane, tpl, active, tw);
+    if (nst == 1) {
+        stage_store<RL, kIoFunc, 3>(u, sl, n, 1, lane, tpl, active, io);
+        return;
+    }
+    __syncthreads();  // every thread has read its last forward inputs
+    stage_store<RL, kIoSmem, 3>(u, sl, n, 1, lane, tpl, active, ndst);
+    __syncthreads();
+    ns = RL;
+    for (int s = 1; s < nst; ++s) {
+        const int R = plan_radix<T2>(p, nst - 1 - s);
+        if (s == nst - 1)
+            fft_stage_rt<+1, kIoSmem, kIoFunc, 3>(R, sl, n, ns, lane, tpl, active, tw, nsrc, io);
+        else
+            fft_stage_rt<+1, kIoSmem, kIoSmem, 3>(R, sl, n, ns, lane, tpl, active, tw, nsrc, ndst);
+        ns *= R;
+    }
+}
 
 // ZMODE: 0 = forward z, Green multiply, inverse z; 1 = forward z only;
 // 2 = inverse z only
 template <typename T, int ZMODE>
-__global__ void __launch_bounds__(sizeof(T) == 8 ? 256 : 512) k_zgreen(ZArgs a) {
+__global__ void __launch_bounds__(256) k_zgreen(ZArgs a) {
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T2* lines = reinterpret_cast<T2*>(smem_raw);
-    const int nz = a.nz;
-    const int k0 = blockIdx.x * a.tz;
-    const int tz = min(a.tz, a.nxh - k0);
-    const long long ky = blockIdx.y;
-    const long long plane = (long long)a.ny * a.nxh;
-    T2* spec = reinterpret_cast<T2*>(a.spec);
-    const long long off0 = ky * a.nxh + k0;
-    const int total = 3 * nz * tz;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int c = t % tz;
-        const int rest = t / tz;
-        const int z = rest % nz;
-        const int comp = rest / nz;
-        lines[(comp * tz + c) * nz + z] = spec[comp * a.nh + z * plane + off0 + c];
-    }
-    __syncthreads();
-    const int tpl = a.plan.tpl;
-    const int q = threadIdx.x / tpl;
-    const int lane = threadIdx.x - q * tpl;
-    T2* my = q < 3 * tz ? lines + q * nz : (T2*)nullptr;
-    if (ZMODE != 2) fft_line<-1>(my, a.plan, lane);
-    // Green multiply: u = G f at every (kz, kx)
-    const T* g = reinterpret_cast<const T*>(a.green);
-    for (int t = threadIdx.x; ZMODE == 0 && t < nz * tz; t += blockDim.x) {
-        const int c = t % tz;
-        const int z = t / tz;
-        const long long gi = z * plane + off0 + c;
-        const T gxx = g[gi], gxy = g[a.nh + gi], gxz = g[2 * a.nh + gi];
-        const T gyy = g[3 * a.nh + gi], gyz = g[4 * a.nh + gi], gzz = g[5 * a.nh + gi];
-        T2* fx = &lines[(0 * tz + c) * nz + z];
-        T2* fy = &lines[(1 * tz + c) * nz + z];
-        T2* fz = &lines[(2 * tz + c) * nz + z];
-        const T2 ax = *fx, ay = *fy, az = *fz;
-        *fx = cmk<T2>(gxx * ax.x + gxy * ay.x + gxz * az.x, gxx * ax.y + gxy * ay.y + gxz * az.y);
-        *fy = cmk<T2>(gxy * ax.x + gyy * ay.x + gyz * az.x, gxy * ax.y + gyy * ay.y + gyz * az.y);
-        *fz = cmk<T2>(gxz * ax.x + gyz * ay.x + gzz * az.x, gxz * ax.y + gyz * ay.y + gzz * az.y);
-    }
-    __syncthreads();
-    if (ZMODE != 1) fft_line<+1>(my, a.plan, lane);
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int c = t % tz;
-        const int rest = t / tz;
-        const int z = rest % nz;
-        const int comp = rest / nz;
-        spec[comp * a.nh + z * plane + off0 + c] = lines[(comp * tz + c) * nz + z];
+    const int tz = a.tz;
+    const int k0 = blockIdx.x * tz;
+    const int c = threadIdx.x % tz;
+    const int lane = threadIdx.x / tz;
+    const bool active = (k0 + c) < a.nxh;
+    ColIo<T2> io;
+    io.base = reinterpret_cast<T2*>(a.spec) + (long long)blockIdx.y * a.rs + k0 + (active ? c : 0);
+    io.cstride = a.nh;
+    io.estride = a.plane;
+    T2* sl[3];
+#pragma unroll
+    for (int l = 0; l < 3; ++l) sl[l] = lines + (l * tz + c) * a.ld;
+    if (ZMODE == 1) {
+        fft_lines<-1, kIoFunc, kIoFunc, 3>(sl, a.plan, lane, active, false, io, io);
+    } else if (ZMODE == 2) {
+        fft_lines<+1, kIoFunc, kIoFunc, 3>(sl, a.plan, lane, active, false, io, io);
+    } else {
+        const int nst = plan_nstage<T2>(a.plan);
+        if (nst == 0) {  // nz == 1: the z transforms are identities
+            if (active && lane == 0) {
+                const T* g = reinterpret_cast<const T*>(a.green);
+                const long long gi = (long long)blockIdx.y * a.rs + k0 + c;
+                const T gxx = g[gi], gxy = g[a.gstride + gi], gxz = g[2 * a.gstride + gi];
+                const T gyy = g[3 * a.gstride + gi], gyz = g[4 * a.gstride + gi];
+                const T gzz = g[5 * a.gstride + gi];
+                const T2 ax = io(0, 0), ay = io(1, 0), az = io(2, 0);
+                io(0, 0, cmk<T2>(gxx * ax.x + gxy * ay.x + gxz * az.x, gxx * ax.y + gxy * ay.y + gxz * az.y));
+                io(1, 0, cmk<T2>(gxy * ax.x + gyy * ay.x + gyz * az.x, gxy * ax.y + gyy * ay.y + gyz * az.y));
+                io(2, 0, cmk<T2>(gxz * ax.x + gyz * ay.x + gzz * az.x, gxz * ax.y + gyz * ay.y + gzz * az.y));
+            }
+            return;
+        }
+        switch (plan_radix<T2>(a.plan, nst - 1)) {
+            case 16:
+                if constexpr (sizeof(T) == 4) z_fused<16, T>(a, sl, io, c, lane, active);
+                break;
+            case 8: z_fused<8, T>(a, sl, io, c, lane, active); break;
+            case 4: z_fused<4, T>(a, sl, io, c, lane, active); break;
+            case 2: z_fused<2, T>(a, sl, io, c, lane, active); break;
+            case 3: z_fused<3, T>(a, sl, io, c, lane, active); break;
+            default: z_fused<5, T>(a, sl, io, c, lane, active); break;
+        }
     }
 }
 
@@ -351,7 +467,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 256 : 512) k_zgreen(ZArgs a) 
 // ---------------------------------------------------------------------------
 
 template <typename T, int DST>
-__global__ void __launch_bounds__(sizeof(T) == 8 ? 256 : 512) k_xinv(XArgs a) {
+__global__ void __launch_bounds__(256, 3) k_xinv(XArgs a) {
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -359,6 +475,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 256 : 512) k_xinv(XArgs a) {
     __shared__ double red[4 * 32];
     const int nx = a.nx;
     const int nxh = a.nxh;
+    const int ld = a.ld;
     const long long r0 = (long long)blockIdx.x * a.rows_per_cta;
     const int rows = (int)min((long long)a.rows_per_cta, a.nrows - r0);
     const int nreal = 3 * rows;
@@ -366,42 +483,55 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 256 : 512) k_xinv(XArgs a) {
     const T2* spec = reinterpret_cast<const T2*>(a.spec);
     const bool even = (nx % 2) == 0;
 
-    // 1) Z = A + iB on the full line from the two Hermitian half spectra
+    // 1) Z = A + iB on the full line from the two Hermitian half spectra.
+    //    Four (A, B) pairs are loaded per thread before any is used, so that
+    //    eight independent loads are in flight per thread.
     const int tot = nq * nxh;
-    for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-        const int q = t / nxh;
-        const int k = t - q * nxh;
-        T2 A, B;
-        {
-            const int L = 2 * q;
-            const int rl = L / 3;
-            const int c = L - 3 * rl;
-            A = spec[c * a.nh + (r0 + rl) * nxh + k];
-        }
-        {
-            const int L = 2 * q + 1;
-            if (L < nreal) {
-                const int rl = L / 3;
-                const int c = L - 3 * rl;
-                B = spec[c * a.nh + (r0 + rl) * nxh + k];
-            } else {
-                B = cmk<T2>((T)0, (T)0);
+    constexpr int U = 4;
+    for (int t0 = threadIdx.x; t0 < tot; t0 += U * blockDim.x) {
+        T2 A[U], B[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int t = t0 + u * blockDim.x;
+            A[u] = cmk<T2>((T)0, (T)0);
+            B[u] = cmk<T2>((T)0, (T)0);
+            if (t < tot) {
+                const int q = t / nxh;
+                const int k = t - q * nxh;
+                const int La = 2 * q, rla = La / 3, ca = La - 3 * rla;
+                A[u] = spec[ca * a.nh + (r0 + rla) * a.rs + k];
+                const int Lb = La + 1;
+                if (Lb < nreal) {
+                    const int rlb = Lb / 3, cb = Lb - 3 * rlb;
+                    B[u] = spec[cb * a.nh + (r0 + rlb) * a.rs + k];
+                }
             }
         }
-        if (k == 0 || (even && 2 * k == nx)) {  // DC / Nyquist are real for a real line
-            A.y = 0;
-            B.y = 0;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int t = t0 + u * blockDim.x;
+            if (t < tot) {
+                const int q = t / nxh;
+                const int k = t - q * nxh;
+                T2 Av = A[u], Bv = B[u];
+                if (k == 0 || (even && 2 * k == nx)) {  // DC / Nyquist are real for a real line
+                    Av.y = 0;
+                    Bv.y = 0;
+                }
+                lines[q * ld + pidx<T2>(k)] = cmk<T2>(Av.x - Bv.y, Av.y + Bv.x);
+                const int kn = nx - k;
+                if (k > 0 && kn >= nxh) lines[q * ld + pidx<T2>(kn)] = cmk<T2>(Av.x + Bv.y, Bv.x - Av.y);
+            }
         }
-        lines[q * nx + k] = cmk<T2>(A.x - B.y, A.y + B.x);
-        const int kn = nx - k;
-        if (k > 0 && kn >= nxh) lines[q * nx + kn] = cmk<T2>(A.x + B.y, B.x - A.y);
     }
     __syncthreads();
     {
-        const int tpl = a.plan.tpl;
+        const int tpl = plan_tpl<T2>(a.plan);
         const int q = threadIdx.x / tpl;
         const int lane = threadIdx.x - q * tpl;
-        fft_line<+1>(q < nq ? lines + q * nx : (T2*)nullptr, a.plan, lane);
+        T2* my = lines + (q < nq ? q : 0) * ld;
+        fft_lines<+1, kIoSmem, kIoSmem, 1>(&my, a.plan, lane, q < nq, false, NoSrc<T2>{},
+                                            NoDst<T2>{});
     }
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     if (DST == kDstCompact) {
@@ -414,7 +544,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 256 : 512) k_xinv(XArgs a) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 const int L = 3 * rl + c;
-                const T2 zv = lines[(L >> 1) * nx + x];
+                const T2 zv = lines[(L >> 1) * ld + pidx<T2>(x)];
                 const double val = (double)((L & 1) ? zv.y : zv.x) * a.scale;
                 a.dst[3LL * s + c] = val;
                 acc[c] += val;
@@ -428,7 +558,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 256 : 512) k_xinv(XArgs a) {
             const int x = t - L * nx;
             const int rl = L / 3;
             const int c = L - 3 * rl;
-            const T2 zv = lines[(L >> 1) * nx + x];
+            const T2 zv = lines[(L >> 1) * ld + pidx<T2>(x)];
             const double val = (double)((L & 1) ? zv.y : zv.x) * a.scale;
             a.dst[c * a.n + (r0 + rl) * nx + x] = val;
             acc[c] += val;
@@ -446,15 +576,13 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 256 : 512) k_xinv(XArgs a) {
 // host launcher
 // ---------------------------------------------------------------------------
 
-static int choose_rows_per_cta(const Problem& P, size_t elem, int max_threads) {
-    const int tpl = P.px.dev.tpl;
+static int choose_rows_per_cta(const Problem& P, int tpl, int ld, size_t elem) {
     int rows = 1;
     for (int r = 1; r <= 64; ++r) {
         const int nq = (3 * r + 1) / 2;
-        if (nq * tpl > max_threads) break;
-        if ((size_t)nq * P.nx * elem > 64 * 1024) break;
+        if (nq * tpl > 256) break;  // matches __launch_bounds__(256, 3)
+        if ((size_t)nq * ld * elem > 72 * 1024) break;
         rows = r;
-        if (nq * tpl >= max_threads / 2 && (r % 2) == 0) break;
     }
     if (rows > P.nrows) rows = (int)P.nrows;
     // enough CTAs to fill the machine
@@ -466,16 +594,26 @@ template <typename T>
 static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     using T2 = c_t<T>;
     const size_t elem = sizeof(T2);
-    const int max_threads = sizeof(T) == 8 ? 256 : 512;  // matches __launch_bounds__
+    const bool dbl = sizeof(T) == 8;
+    const int padsh = dbl ? Prec<double2>::PADSH : Prec<float2>::PADSH;
+    const int max_yz = 256;  // matches __launch_bounds__ of the y and z passes
+    auto tpl_of = [&](const AxisPlan& ap) { return dbl ? ap.dev.tpl64 : ap.dev.tpl32; };
+    const long long rs = P.nxh;
+    *nparts = 0;
+
+    // ---- x passes
     XArgs x{};
     x.nx = P.nx;
     x.ny = P.ny;
     x.nz = P.nz;
     x.nxh = P.nxh;
+    x.ld = line_stride(P.nx, padsh);
+    x.rs = rs;
     x.n = P.n;
     x.nh = P.nh;
     x.nrows = P.nrows;
-    x.rows_per_cta = choose_rows_per_cta(P, elem, max_threads);
+    const int tplx = tpl_of(P.px);
+    x.rows_per_cta = choose_rows_per_cta(P, tplx, x.ld, elem);
     x.plan = P.px.dev;
     x.support = P.d_support;
     x.row_ptr = P.d_row_ptr;
@@ -493,92 +631,84 @@ static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     x.partials = P.d_partials;
     x.spec = P.d_spec;
     x.skip = aa.skip;
-
     const int nq = (3 * x.rows_per_cta + 1) / 2;
-    const int xthreads = std::max(32, ((nq * P.px.dev.tpl + 31) / 32) * 32);
-    const size_t xsmem = (size_t)nq * P.nx * elem;
+    const int xthreads = std::max(32, ((nq * tplx + 31) / 32) * 32);
+    const size_t xsmem = (size_t)nq * x.ld * elem;
     const int xblocks = (int)((P.nrows + x.rows_per_cta - 1) / x.rows_per_cta);
 
-    if (aa.stage != kStageInverse) switch (aa.src_kind) {
-        case kSrcCompact:
-            cudaFuncSetAttribute(k_xfwd<T, kSrcCompact>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xsmem);
-            k_xfwd<T, kSrcCompact><<<xblocks, xthreads, xsmem, P.stream>>>(x);
-            break;
-        case kSrcDense:
-            cudaFuncSetAttribute(k_xfwd<T, kSrcDense>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xsmem);
-            k_xfwd<T, kSrcDense><<<xblocks, xthreads, xsmem, P.stream>>>(x);
-            break;
-        case kSrcF0:
-            cudaFuncSetAttribute(k_xfwd<T, kSrcF0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xsmem);
-            k_xfwd<T, kSrcF0><<<xblocks, xthreads, xsmem, P.stream>>>(x);
-            break;
-        default:
-            cudaFuncSetAttribute(k_xfwd<T, kSrcF0Compact>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xsmem);
-            k_xfwd<T, kSrcF0Compact><<<xblocks, xthreads, xsmem, P.stream>>>(x);
-            break;
-    }
-
-    // y passes
+    // ---- y passes: tx columns x 3 components per CTA
     YArgs y{};
     y.ny = P.ny;
     y.nxh = P.nxh;
     y.nh = P.nh;
+    y.rs = rs;
     y.plan = P.py.dev;
     y.spec = P.d_spec;
     y.skip = aa.skip;
+    y.ld = line_stride(P.ny, padsh);
+    const int tply = tpl_of(P.py);
     {
-        int tx = (elem == 16) ? 8 : 16;
-        while (tx > 1 && (tx * P.py.dev.tpl > max_threads || (size_t)tx * P.ny * elem > 64 * 1024)) tx /= 2;
+        int tx = P.tile_yz > 0 ? P.tile_yz : (dbl ? 8 : 16);
+        while (tx > 1 && (tx * tply > max_yz || (size_t)3 * tx * y.ld * elem > 110 * 1024)) tx /= 2;
         y.tx = tx;
     }
-    const int ythreads = std::max(32, ((y.tx * P.py.dev.tpl + 31) / 32) * 32);
-    const size_t ysmem = (size_t)y.tx * P.ny * elem;
-    dim3 ygrid((P.nxh + y.tx - 1) / y.tx, P.nz, 3);
-    cudaFuncSetAttribute(k_ypass<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ysmem);
-    cudaFuncSetAttribute(k_ypass<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ysmem);
-    if (P.ny > 1 && aa.stage != kStageInverse) k_ypass<T, -1><<<ygrid, ythreads, ysmem, P.stream>>>(y);
+    const int ythreads = y.tx * tply;
+    const size_t ysmem = (size_t)3 * y.tx * y.ld * elem;
+    dim3 ygrid((P.nxh + y.tx - 1) / y.tx, P.nz);
 
-    // z pass with the Green multiply
+    // ---- z pass
     ZArgs z{};
     z.ny = P.ny;
     z.nz = P.nz;
     z.nxh = P.nxh;
     z.nh = P.nh;
+    z.rs = rs;
+    z.plane = (long long)P.ny * rs;
+    z.gstride = P.nh;
     z.plan = P.pz.dev;
-    z.green = (sizeof(T) == 8) ? (const void*)P.d_green64 : (const void*)P.d_green32;
+    z.green = dbl ? (const void*)P.d_green64 : (const void*)P.d_green32;
     z.spec = P.d_spec;
     z.skip = aa.skip;
+    z.ld = line_stride(P.nz, padsh);
+    const int tplz = tpl_of(P.pz);
     {
-        int tz = (elem == 16) ? 4 : 8;
-        while (tz > 1 && (3 * tz * P.pz.dev.tpl > max_threads || (size_t)3 * tz * P.nz * elem > 96 * 1024)) tz /= 2;
+        int tz = P.tile_yz > 0 ? P.tile_yz : (dbl ? 8 : 16);
+        while (tz > 1 && (tz * tplz > max_yz || (size_t)3 * tz * z.ld * elem > 110 * 1024)) tz /= 2;
         z.tz = tz;
     }
-    const int zthreads = std::max(32, ((3 * z.tz * P.pz.dev.tpl + 31) / 32) * 32);
-    const size_t zsmem = (size_t)3 * z.tz * P.nz * elem;
+    const int zthreads = z.tz * tplz;
+    const size_t zsmem = (size_t)3 * z.tz * z.ld * elem;
     dim3 zgrid((P.nxh + z.tz - 1) / z.tz, P.ny);
+
+#define FP_LAUNCH(kern, grid, threads, smem, args)                                              \
+    do {                                                                                          \
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem));     \
+        kern<<<grid, threads, smem, P.stream>>>(args);                                            \
+    } while (0)
+
     if (aa.stage != kStageInverse) {
+        switch (aa.src_kind) {
+            case kSrcCompact: FP_LAUNCH((k_xfwd<T, kSrcCompact>), xblocks, xthreads, xsmem, x); break;
+            case kSrcDense: FP_LAUNCH((k_xfwd<T, kSrcDense>), xblocks, xthreads, xsmem, x); break;
+            case kSrcF0: FP_LAUNCH((k_xfwd<T, kSrcF0>), xblocks, xthreads, xsmem, x); break;
+            default: FP_LAUNCH((k_xfwd<T, kSrcF0Compact>), xblocks, xthreads, xsmem, x); break;
+        }
+        if (P.ny > 1) FP_LAUNCH((k_ypass<T, -1>), ygrid, ythreads, ysmem, y);
         if (aa.stage == kStageForward) {
-            cudaFuncSetAttribute(k_zgreen<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zsmem);
-            k_zgreen<T, 1><<<zgrid, zthreads, zsmem, P.stream>>>(z);
-            *nparts = 0;
+            FP_LAUNCH((k_zgreen<T, 1>), zgrid, zthreads, zsmem, z);
             return cudaGetLastError();
         }
-        cudaFuncSetAttribute(k_zgreen<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zsmem);
-        k_zgreen<T, 0><<<zgrid, zthreads, zsmem, P.stream>>>(z);
+        FP_LAUNCH((k_zgreen<T, 0>), zgrid, zthreads, zsmem, z);
     } else {
-        cudaFuncSetAttribute(k_zgreen<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zsmem);
-        k_zgreen<T, 2><<<zgrid, zthreads, zsmem, P.stream>>>(z);
+        FP_LAUNCH((k_zgreen<T, 2>), zgrid, zthreads, zsmem, z);
     }
-
-    if (P.ny > 1) k_ypass<T, +1><<<ygrid, ythreads, ysmem, P.stream>>>(y);
-
+    if (P.ny > 1) FP_LAUNCH((k_ypass<T, +1>), ygrid, ythreads, ysmem, y);
     if (aa.dst_kind == kDstCompact) {
-        cudaFuncSetAttribute(k_xinv<T, kDstCompact>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xsmem);
-        k_xinv<T, kDstCompact><<<xblocks, xthreads, xsmem, P.stream>>>(x);
+        FP_LAUNCH((k_xinv<T, kDstCompact>), xblocks, xthreads, xsmem, x);
     } else {
-        cudaFuncSetAttribute(k_xinv<T, kDstDense>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xsmem);
-        k_xinv<T, kDstDense><<<xblocks, xthreads, xsmem, P.stream>>>(x);
+        FP_LAUNCH((k_xinv<T, kDstDense>), xblocks, xthreads, xsmem, x);
     }
+#undef FP_LAUNCH
     *nparts = xblocks;
     return cudaGetLastError();
 }

@@ -159,19 +159,23 @@ cudaError_t launch_support(Problem& P) {
 // G(k) = sum_{|p_i| <= P} prod_i sinc^2(pi m_i / n_i) (1/(mu q^2)) (I - q q^T / q^2)
 // with unshifted m_i = k_i + p_i n_i, k_i in [0, n_i), q_i = 2 pi m_i / L_i,
 // L_i = h n_i, terms with zero weight or q^2 <= DBL_EPSILON skipped, G(0) = 0.
-// The per-axis factors sinc(pi m/n) and q are tabulated on the host with the
-// reference's own expressions; the sums run in the reference's order with
-// explicitly rounded operations (no FMA contraction), so each G(k) equals the
-// reference's value.  The table stores the symmetrised
-// Gs(k) = (G(k) + G(-k)) / 2 on the half spectrum kx in [0, nx/2]: the
-// reference keeps only Re(IFFT(G * F)), which is the IFFT of Gs * F.
+//
+// The table holds the symmetrised Gs(k) = (G(k) + G(-k)) / 2 on the half
+// spectrum kx in [0, nx/2]: the reference keeps only Re(IFFT(G * F)), which is
+// the IFFT of Gs * F.  Because a term depends on m only through m m^T and
+// |m|^2, G(-k) is the sum over the same terms m = k + p n with the window
+// p_i in [-P-1, P-1] on every axis where k_i != 0 (and [-P, P] where k_i = 0).
+// One loop over the union window [-P-1, P]^3 therefore evaluates each term
+// once with coefficient ([p in W^3] + [p in W'^3]) / 2.
+// The per-axis factors sinc(pi m/n) and q_i are tabulated on the host with the
+// reference's own expressions.
 // ---------------------------------------------------------------------------
 
 struct GreenArgs {
-    int nx, ny, nz, nxh, np;  // np = 2P + 1
+    int nx, ny, nz, nxh, nw, pr;  // nw = 2P + 2 table entries per k: p = -P-1 .. P
     double mu;
-    const double* sx;  // [nx][np] sinc values
-    const double* qx;  // [nx][np]
+    const double* sx;  // [n][nw] sinc(pi m / n)
+    const double* qx;  // [n][nw] 2 pi m / L
     const double* sy;
     const double* qy;
     const double* sz;
@@ -181,43 +185,6 @@ struct GreenArgs {
     long long nh;
 };
 
-__device__ __forceinline__ void green_sum(const GreenArgs& a, int kx, int ky, int kz, double g[6]) {
-    for (int i = 0; i < 6; ++i) g[i] = 0.0;
-    if (kx == 0 && ky == 0 && kz == 0) return;
-    const double* sxr = a.sx + (long long)kx * a.np;
-    const double* qxr = a.qx + (long long)kx * a.np;
-    const double* syr = a.sy + (long long)ky * a.np;
-    const double* qyr = a.qy + (long long)ky * a.np;
-    const double* szr = a.sz + (long long)kz * a.np;
-    const double* qzr = a.qz + (long long)kz * a.np;
-    for (int ix = 0; ix < a.np; ++ix) {
-        const double sx = sxr[ix], qx = qxr[ix];
-        const double wx = __dmul_rn(sx, sx);
-        const double qxx = __dmul_rn(qx, qx);
-        for (int iy = 0; iy < a.np; ++iy) {
-            const double sy = syr[iy], qy = qyr[iy];
-            const double wxy = __dmul_rn(wx, __dmul_rn(sy, sy));
-            const double qxy2 = __dadd_rn(qxx, __dmul_rn(qy, qy));
-            for (int iz = 0; iz < a.np; ++iz) {
-                const double sz = szr[iz], qz = qzr[iz];
-                const double weight = __dmul_rn(wxy, __dmul_rn(sz, sz));
-                if (weight == 0.0) continue;
-                const double q2 = __dadd_rn(qxy2, __dmul_rn(qz, qz));
-                if (q2 <= DBL_EPSILON) continue;
-                const double inv_mu_q2 = __ddiv_rn(1.0, __dmul_rn(a.mu, q2));
-                const double inv_q2 = __ddiv_rn(1.0, q2);
-                const double fac = __dmul_rn(weight, inv_mu_q2);
-                g[0] = __dadd_rn(g[0], __dmul_rn(fac, __dsub_rn(1.0, __dmul_rn(qxx, inv_q2))));
-                g[1] = __dadd_rn(g[1], __dmul_rn(fac, __dmul_rn(__dmul_rn(-qx, qy), inv_q2)));
-                g[2] = __dadd_rn(g[2], __dmul_rn(fac, __dmul_rn(__dmul_rn(-qx, qz), inv_q2)));
-                g[3] = __dadd_rn(g[3], __dmul_rn(fac, __dsub_rn(1.0, __dmul_rn(__dmul_rn(qy, qy), inv_q2))));
-                g[4] = __dadd_rn(g[4], __dmul_rn(fac, __dmul_rn(__dmul_rn(-qy, qz), inv_q2)));
-                g[5] = __dadd_rn(g[5], __dmul_rn(fac, __dsub_rn(1.0, __dmul_rn(__dmul_rn(qz, qz), inv_q2))));
-            }
-        }
-    }
-}
-
 __global__ void k_green(GreenArgs a) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.nh) return;
@@ -225,16 +192,64 @@ __global__ void k_green(GreenArgs a) {
     const long long rest = t / a.nxh;
     const int ky = (int)(rest % a.ny);
     const int kz = (int)(rest / a.ny);
-    double g[6], gb[6];
-    green_sum(a, kx, ky, kz, g);
-    const int bx = kx == 0 ? 0 : a.nx - kx;
-    const int by = ky == 0 ? 0 : a.ny - ky;
-    const int bz = kz == 0 ? 0 : a.nz - kz;
-    green_sum(a, bx, by, bz, gb);
+    double s0 = 0, sxx = 0, syy = 0, szz = 0, sxy = 0, sxz = 0, syz = 0;
+    if (!(kx == 0 && ky == 0 && kz == 0)) {
+        const int P = a.pr;
+        const double* sxr = a.sx + (long long)kx * a.nw;
+        const double* qxr = a.qx + (long long)kx * a.nw;
+        const double* syr = a.sy + (long long)ky * a.nw;
+        const double* qyr = a.qy + (long long)ky * a.nw;
+        const double* szr = a.sz + (long long)kz * a.nw;
+        const double* qzr = a.qz + (long long)kz * a.nw;
+        const double inv_mu = 1.0 / a.mu;
+        for (int ix = 0; ix < a.nw; ++ix) {
+            const int px = ix - P - 1;
+            // membership of p in W = [-P, P] and in W' (shifted where k != 0)
+            const int ax = (px >= -P);
+            const int bx = kx != 0 ? (px <= P - 1) : ax;
+            if (!(ax | bx)) continue;
+            const double wx = sxr[ix] * sxr[ix];
+            const double qxv = qxr[ix];
+            const double qxx = qxv * qxv;
+            for (int iy = 0; iy < a.nw; ++iy) {
+                const int py = iy - P - 1;
+                const int ay = ax & (py >= -P);
+                const int by = bx & (ky != 0 ? (py <= P - 1) : (py >= -P));
+                if (!(ay | by)) continue;
+                const double wxy = wx * (syr[iy] * syr[iy]);
+                const double qyv = qyr[iy];
+                const double qyy = qyv * qyv;
+                const double qxy2 = qxx + qyy;
+                const double qxqy = qxv * qyv;
+                for (int iz = 0; iz < a.nw; ++iz) {
+                    const int pz = iz - P - 1;
+                    const int az = ay & (pz >= -P);
+                    const int bz = by & (kz != 0 ? (pz <= P - 1) : (pz >= -P));
+                    const int cnt = az + bz;
+                    if (cnt == 0) continue;
+                    const double weight = wxy * (szr[iz] * szr[iz]);
+                    if (weight == 0.0) continue;
+                    const double qzv = qzr[iz];
+                    const double q2 = qxy2 + qzv * qzv;
+                    if (q2 <= DBL_EPSILON) continue;
+                    const double inv_q2 = __drcp_rn(q2);
+                    const double fac = (0.5 * cnt) * weight * inv_q2 * inv_mu;
+                    const double f2 = fac * inv_q2;
+                    s0 += fac;
+                    sxx += f2 * qxx;
+                    syy += f2 * qyy;
+                    szz += f2 * (qzv * qzv);
+                    sxy += f2 * qxqy;
+                    sxz += f2 * (qxv * qzv);
+                    syz += f2 * (qyv * qzv);
+                }
+            }
+        }
+    }
+    const double g[6] = {s0 - sxx, -sxy, -sxz, s0 - syy, -syz, s0 - szz};
     for (int c = 0; c < 6; ++c) {
-        const double v = 0.5 * (g[c] + gb[c]);
-        if (a.g64) a.g64[c * a.nh + t] = v;
-        if (a.g32) a.g32[c * a.nh + t] = (float)v;
+        if (a.g64) a.g64[c * a.nh + t] = g[c];
+        if (a.g32) a.g32[c * a.nh + t] = (float)g[c];
     }
 }
 
@@ -243,19 +258,20 @@ static double host_sinc(double x) {
     return std::sin(x) / x;
 }
 
-cudaError_t launch_green(Problem& P) {
+cudaError_t launch_green(Problem& P, double* g64, float* g32) {
     const int Pr = P.p_radius < 0 ? 0 : P.p_radius;
-    const int np = 2 * Pr + 1;
+    const int nw = 2 * Pr + 2;
     const double kPi = 3.14159265358979323846;
     auto tab = [&](int n, std::vector<double>& s, std::vector<double>& q) {
         const double L = P.h * (double)n;
-        s.resize((size_t)n * np);
-        q.resize((size_t)n * np);
+        s.resize((size_t)n * nw);
+        q.resize((size_t)n * nw);
         for (int k = 0; k < n; ++k)
-            for (int p = -Pr; p <= Pr; ++p) {
-                const long long m = (long long)k + (long long)p * n;
-                s[(size_t)k * np + (p + Pr)] = host_sinc(kPi * (double)m / (double)n);
-                q[(size_t)k * np + (p + Pr)] = (2.0 * kPi * (double)m) / L;
+            for (int i = 0; i < nw; ++i) {
+                const long long p = i - Pr - 1;
+                const long long m = (long long)k + p * n;
+                s[(size_t)k * nw + i] = host_sinc(kPi * (double)m / (double)n);
+                q[(size_t)k * nw + i] = (2.0 * kPi * (double)m) / L;
             }
     };
     std::vector<double> hsx, hqx, hsy, hqy, hsz, hqz;
@@ -283,7 +299,8 @@ cudaError_t launch_green(Problem& P) {
     a.ny = P.ny;
     a.nz = P.nz;
     a.nxh = P.nxh;
-    a.np = np;
+    a.nw = nw;
+    a.pr = Pr;
     a.mu = P.mu;
     a.sx = dsx;
     a.qx = dqx;
@@ -291,8 +308,8 @@ cudaError_t launch_green(Problem& P) {
     a.qy = dqy;
     a.sz = dsz;
     a.qz = dqz;
-    a.g64 = P.d_green64;
-    a.g32 = P.d_green32;
+    a.g64 = g64;
+    a.g32 = g32;
     a.nh = P.nh;
     const int threads = 128;
     const long long blocks = (P.nh + threads - 1) / threads;

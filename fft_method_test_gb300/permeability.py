@@ -344,3 +344,60 @@ class PermeabilityTensor:
 
     def data(self) -> np.ndarray:
         return self.k
+
+
+# ---------------------------------------------------------------------------
+# Brinkman penalisation (include/brinkman/FluidBrinkman.hpp:45-55)
+# ---------------------------------------------------------------------------
+
+def _brinkman_check(lib, rc):
+    if rc == _capi.FP_OK:
+        return
+    msg = lib.fp_brinkman_last_error().decode()
+    if rc == _capi.FP_ERR_INVALID:
+        raise ValueError(msg)
+    raise _capi.FpError(rc, msg)
+
+
+def solveBrinkman(ids: np.ndarray, force, fluid_id: int = 1, fluid_mu: float = 1.0,
+                  solid_penalty: float = 1.0e8, relaxation: float = 0.9,
+                  tolerance: float = 1.0e-8, max_iterations: int = 600,
+                  want_fields: bool = False) -> dict:
+    """common::fluid::solveBrinkman on the GPU.  ids: material ids (nz, ny, nx);
+    defaults are the reference's FluidConfig defaults (Config.hpp:33-47)."""
+    lib = _capi.load()
+    ids = np.ascontiguousarray(ids, dtype=np.uint32)
+    nz, ny, nx = ids.shape
+    n = ids.size
+    fields = [np.zeros(n) for _ in range(4)] if want_fields else None
+    U = np.zeros(3)
+    st = _capi.BrinkmanStats()
+    ptrs = [f.ctypes.data for f in fields] if want_fields else [None] * 4
+    rc = lib.fp_brinkman_solve(nx, ny, nz, ids.ravel(), int(fluid_id), float(fluid_mu),
+                               float(solid_penalty), float(relaxation), float(tolerance),
+                               int(max_iterations), np.asarray(force, np.float64), *ptrs, U,
+                               C.byref(st))
+    _brinkman_check(lib, rc)
+    out = dict(superficialVelocity=U, **st.as_dict())
+    if want_fields:
+        out.update(ux=fields[0].reshape(ids.shape), uy=fields[1].reshape(ids.shape),
+                   uz=fields[2].reshape(ids.shape), p=fields[3].reshape(ids.shape))
+    return out
+
+
+def computePermeabilityTensor(ids: np.ndarray, fluid_id: int = 1, fluid_mu: float = 1.0,
+                              solid_penalty: float = 1.0e8, relaxation: float = 0.9,
+                              tolerance: float = 1.0e-8, max_iterations: int = 600,
+                              forcing: float = 1.0, voxel_size: float = 1.0):
+    """common::fluid::computePermeabilityTensor on the GPU: (K 3x3, [stats] * 3)."""
+    lib = _capi.load()
+    ids = np.ascontiguousarray(ids, dtype=np.uint32)
+    nz, ny, nx = ids.shape
+    K = np.zeros(9)
+    stats = (_capi.BrinkmanStats * 3)()
+    rc = lib.fp_brinkman_permeability(nx, ny, nz, ids.ravel(), int(fluid_id), float(fluid_mu),
+                                      float(solid_penalty), float(relaxation), float(tolerance),
+                                      int(max_iterations), float(forcing), float(voxel_size), K,
+                                      stats)
+    _brinkman_check(lib, rc)
+    return K.reshape(3, 3), [s.as_dict() for s in stats]

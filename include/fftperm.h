@@ -128,6 +128,39 @@ int fp_solve_load_case(fp_handle h, const double grad[3], const double* x0, doub
 int fp_solve_permeability(fp_handle h, double tol, int64_t maxit, double K[9],
                           fp_solver_stats stats[3]);
 
+/* ---- Brinkman penalisation (src/brinkman/FluidBrinkman.cpp) ---------------- */
+
+typedef struct fp_brinkman_stats {
+    int32_t iterations; /* SolveDiagnostics::iterations (include/brinkman/FluidBrinkman.hpp:16-21) */
+    int32_t converged;  /* SolveDiagnostics::converged */
+    double residual;    /* SolveDiagnostics::residual: sqrt(sum div(u*)^2 / N) */
+    double porosity;    /* SolveResult::porosity */
+    double viscosity;   /* SolveResult::viscosity (mean fluid viscosity) */
+    double seconds;     /* SolveDiagnostics::elapsedSeconds */
+} fp_brinkman_stats;
+
+/* common::fluid::solveBrinkman (include/brinkman/FluidBrinkman.hpp:45-49,
+ * src/brinkman/FluidBrinkman.cpp:282-507): the reference's relaxed-Jacobi
+ * momentum + 35-sweep pressure projection, FP64, from rest.  ids holds one
+ * material id per voxel; ids == fluid_id is fluid of viscosity fluid_mu, any
+ * other id is solid (penalty solid_penalty, viscosity 1), as the reference
+ * resolves phases without phase tags.  ux, uy, uz, p (N doubles each) may be
+ * NULL.  U receives the superficial velocity.  Returns FP_ERR_NONFINITE when
+ * the residual becomes non-finite (the reference throws) and FP_ERR_STATE
+ * when the medium has no fluid or no solid voxel.  Messages:
+ * fp_brinkman_last_error(). */
+int fp_brinkman_solve(int nx, int ny, int nz, const uint32_t* ids, uint32_t fluid_id,
+                      double fluid_mu, double solid_penalty, double relaxation, double tolerance,
+                      int max_iterations, const double force[3], double* ux, double* uy,
+                      double* uz, double* p, double U[3], fp_brinkman_stats* stats);
+/* common::fluid::computePermeabilityTensor (src/brinkman/FluidBrinkman.cpp:509-553):
+ * three solves with force = forcing * e_j; K[i*3+j] = mu U_i / f_j * h^2. */
+int fp_brinkman_permeability(int nx, int ny, int nz, const uint32_t* ids, uint32_t fluid_id,
+                             double fluid_mu, double solid_penalty, double relaxation,
+                             double tolerance, int max_iterations, double forcing,
+                             double voxel_size, double K[9], fp_brinkman_stats stats[3]);
+const char* fp_brinkman_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

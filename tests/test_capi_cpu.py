@@ -40,3 +40,25 @@ def test_python_mirror_loads_and_validates_without_gpu():
     assert list(t.data()[[1, 4, 7]]) == [-1.0, -2.0, -3.0]
     with pytest.raises(IndexError):
         t.set_column(3, [0, 0, 0])
+
+
+@pytest.mark.parametrize("precision", ["FFT_METHOD_PRECISION_DOUBLE", "FFT_METHOD_PRECISION_FLOAT"])
+def test_cpp_adapters_compile_against_reference(precision):
+    """The C++ drop-ins (CudaFFTBackend : IFFTBackend, CudaVariationalOperator :
+    ILinearOperator, cuda_solve_one_direction) compile against the reference's
+    own headers in both of its precisions."""
+    import shutil
+    import subprocess
+
+    ref = "/root/reference"
+    if not os.path.isdir(os.path.join(ref, "src")):
+        pytest.skip("reference sources not present on this host")
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("g++ not available")
+    src = os.path.join(ROOT, "fft_method_test_gb300", "host", "CudaBackends.cpp")
+    r = subprocess.run([gxx, "-std=c++20", "-fsyntax-only", "-Wall", "-Wextra", "-Werror",
+                        "-D%s=1" % precision, "-I" + os.path.join(ref, "src"),
+                        "-I" + os.path.join(ref, "include"), "-I" + os.path.join(ROOT, "include"), src],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
