@@ -35,7 +35,7 @@ EXPORTED = [
     "fp_background_force",
     "fp_operator_apply", "fp_operator_apply_device", "fp_build_rhs", "fp_minres", "fp_recover",
     "fp_solve_load_case", "fp_solve_permeability", "fp_brinkman_solve",
-    "fp_brinkman_permeability", "fp_brinkman_last_error",
+    "fp_brinkman_permeability", "fp_brinkman_last_error", "fp_green_apply_noalloc",
 ]
 
 
@@ -107,6 +107,8 @@ _SIGNATURES = {
                                   C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
                                   C.c_double, _dp, C.POINTER(BrinkmanStats)], C.c_int),
     "fp_brinkman_last_error": ([], C.c_char_p),
+    "fp_green_apply_noalloc": ([C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
+                                C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
 }
 
 _lib = None

@@ -106,6 +106,25 @@ struct Problem {
 constexpr int kMaxPartials = 8192;
 
 // ---- setup kernels (kernels_setup.cu) ----
+// Inputs of the Green-table kernel: per-axis tables of sinc(pi m / n) and
+// q = 2 pi m / L for m = k + p n, p = -P-1 .. P (nw = 2P + 2 entries per k).
+struct GreenArgs {
+    int nx, ny, nz, nxh, nw, pr;
+    double mu;
+    const double* sx;  // [nx][nw]
+    const double* qx;
+    const double* sy;
+    const double* qy;
+    const double* sz;
+    const double* qz;
+    double* g64;
+    float* g32;
+    long long nh;
+};
+cudaError_t launch_green_kernel(const GreenArgs& a, cudaStream_t stream);
+// Radix plan of one axis without twiddles (no allocation); false when n does
+// not factor into 2, 3 and 5 or exceeds the supported maximum.
+bool fill_plan_radices(int n, FftPlanDev& d);
 cudaError_t launch_support(Problem& P);
 // Computes the Green table into g64 and/or g32 (either may be null).
 cudaError_t launch_green(Problem& P, double* g64, float* g32);

@@ -56,6 +56,22 @@ static int factor_radices(int n, int* radix, int max_log2) {
     return n == 1 ? k : -1;
 }
 
+bool fill_plan_radices(int n, FftPlanDev& d) {
+    if (n < 1 || n > 640) return false;
+    d.n = n;
+    const int ns32 = factor_radices(n, d.radix32, 4);
+    const int ns64 = factor_radices(n, d.radix64, 3);
+    if (ns32 < 0 || ns64 < 0) return false;
+    d.nstage32 = ns32;
+    d.nstage64 = ns64;
+    int r32 = 1, r64 = 1;
+    for (int i = 0; i < ns32; ++i) r32 = std::max(r32, d.radix32[i]);
+    for (int i = 0; i < ns64; ++i) r64 = std::max(r64, d.radix64[i]);
+    d.tpl32 = (n + r32 - 1) / r32;
+    d.tpl64 = (n + r64 - 1) / r64;
+    return true;
+}
+
 bool make_axis_plan(int n, AxisPlan& p, std::string& err) {
     p = AxisPlan{};
     if (n > 640) {

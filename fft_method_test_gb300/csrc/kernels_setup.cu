@@ -171,20 +171,6 @@ cudaError_t launch_support(Problem& P) {
 // reference's own expressions.
 // ---------------------------------------------------------------------------
 
-struct GreenArgs {
-    int nx, ny, nz, nxh, nw, pr;  // nw = 2P + 2 table entries per k: p = -P-1 .. P
-    double mu;
-    const double* sx;  // [n][nw] sinc(pi m / n)
-    const double* qx;  // [n][nw] 2 pi m / L
-    const double* sy;
-    const double* qy;
-    const double* sz;
-    const double* qz;
-    double* g64;
-    float* g32;
-    long long nh;
-};
-
 __global__ void k_green(GreenArgs a) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.nh) return;
@@ -311,13 +297,17 @@ cudaError_t launch_green(Problem& P, double* g64, float* g32) {
     a.g64 = g64;
     a.g32 = g32;
     a.nh = P.nh;
-    const int threads = 128;
-    const long long blocks = (P.nh + threads - 1) / threads;
-    k_green<<<(unsigned)blocks, threads, 0, P.stream>>>(a);
-    e = cudaGetLastError();
+    e = launch_green_kernel(a, P.stream);
     cudaStreamSynchronize(P.stream);
     cudaFree(d);
     return e;
+}
+
+cudaError_t launch_green_kernel(const GreenArgs& a, cudaStream_t stream) {
+    const int threads = 128;
+    const long long blocks = (a.nh + threads - 1) / threads;
+    k_green<<<(unsigned)blocks, threads, 0, stream>>>(a);
+    return cudaGetLastError();
 }
 
 }  // namespace fp

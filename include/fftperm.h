@@ -128,6 +128,23 @@ int fp_solve_load_case(fp_handle h, const double grad[3], const double* x0, doub
 int fp_solve_permeability(fp_handle h, double tol, int64_t maxit, double K[9],
                           fp_solver_stats stats[3]);
 
+/* No counterpart in the reference.  The Green-operator apply of fp_green_apply
+ * for callers that must not allocate device memory themselves, for example
+ * code running inside another framework's memory manager (which owns the
+ * device heap) or a latency-critical loop that cannot accept the device-wide
+ * synchronisation cudaMalloc/cudaFree may bring.  The caller passes device
+ * pointers to the input force field and the output field (3*N doubles each,
+ * SoA) and a cudaStream_t (NULL = the legacy default stream); the work is
+ * queued on that stream and the call returns without waiting.  FP64.
+ * All working memory is one fixed, file-scope device array of about 14 MB,
+ * so the grid is limited to N <= 262144 voxels (e.g. 64^3), (nx/2+1)*ny*nz <=
+ * 135168 and ny*nz <= 16384; larger grids return FP_ERR_INVALID.  The array is
+ * shared by all calls: calls that overlap on the GPU race and must be
+ * serialised by the caller.  The first call on a device resolves the array's
+ * address; make that first call before any stream capture. */
+int fp_green_apply_noalloc(int nx, int ny, int nz, double voxel_size, double mu, int p_radius,
+                           const double* d_force_soa, double* d_velocity_soa, void* stream);
+
 /* ---- Brinkman penalisation (src/brinkman/FluidBrinkman.cpp) ---------------- */
 
 typedef struct fp_brinkman_stats {
