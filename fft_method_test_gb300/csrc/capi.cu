@@ -70,6 +70,14 @@ int need_geometry(Problem& P, const char* who) {
     return FP_OK;
 }
 
+// A TMA pass whose bounded wait gave up leaves the flag set: report it.
+int check_device_error(Problem& P) {
+    int e = 0;
+    FP_CUDA(cudaMemcpy(&e, P.d_err, sizeof(int), cudaMemcpyDeviceToHost), "error flag copy");
+    if (e) return fail(P, FP_ERR_CUDA, "a TMA wait in an FFT pass timed out");
+    return FP_OK;
+}
+
 int alloc_dense(Problem& P) {
     if (!P.d_dense_in) FP_CUDA(dalloc(&P.d_dense_in, 3 * (size_t)P.n), "cudaMalloc dense");
     if (!P.d_dense_out) FP_CUDA(dalloc(&P.d_dense_out, 3 * (size_t)P.n), "cudaMalloc dense");
@@ -154,6 +162,10 @@ int device_minres(Problem& P, const double* d_b, const double* d_x0, double tol,
         FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
     }
     const fp::MinresScalars s = *P.h_sc;
+    {
+        const int erc = check_device_error(P);
+        if (erc) return erc;
+    }
     if (hist_host) {
         FP_CUDA(cudaMemcpy(hist_host, P.d_hist, sizeof(double) * (size_t)(s.it + 1),
                            cudaMemcpyDeviceToHost),
@@ -233,7 +245,8 @@ int fp_create(int nx, int ny, int nz, double voxel_size, double mu, int p_radius
     P.n = (long long)nx * ny * nz;
     P.nxh = nx / 2 + 1;
     P.nrows = (long long)ny * nz;
-    P.nh = (long long)P.nxh * P.nrows;
+    P.rs = (P.nxh + 1) & ~1LL;
+    P.nh = P.rs * P.nrows;
     P.h = voxel_size;
     P.mu = mu;
     P.p_radius = p_radius < 0 ? 0 : p_radius;
@@ -244,6 +257,7 @@ int fp_create(int nx, int ny, int nz, double voxel_size, double mu, int p_radius
     FP_CUDA(cudaDeviceGetAttribute(&P.sm_count, cudaDevAttrMultiProcessorCount, dev), "attr");
     FP_CUDA(cudaStreamCreateWithFlags(&P.stream, cudaStreamNonBlocking), "stream");
     if (const char* t = std::getenv("FFTPERM_TILE_YZ")) P.tile_yz = std::atoi(t);
+    if (const char* t = std::getenv("FFTPERM_NO_TMA")) P.tma_off = std::atoi(t) != 0;
     std::string err;
     if (!fp::make_axis_plan(nx, P.px, err) || !fp::make_axis_plan(ny, P.py, err) ||
         !fp::make_axis_plan(nz, P.pz, err))
@@ -253,6 +267,8 @@ int fp_create(int nx, int ny, int nz, double voxel_size, double mu, int p_radius
     FP_CUDA(dalloc(&P.d_partials, 4 * nparts), "cudaMalloc partials");
     FP_CUDA(dalloc(&P.d_red, 64), "cudaMalloc red");
     FP_CUDA(dalloc(&P.d_sc, 1), "cudaMalloc scalars");
+    FP_CUDA(dalloc(&P.d_err, 1), "cudaMalloc error flag");
+    FP_CUDA(cudaMemset(P.d_err, 0, sizeof(int)), "memset");
     FP_CUDA(cudaMallocHost(&P.h_sc, sizeof(fp::MinresScalars)), "cudaMallocHost");
     FP_CUDA(dalloc(&P.d_row_ptr, (size_t)P.nrows + 1), "cudaMalloc row_ptr");
     FP_CUDA(dalloc(&P.d_row_cnt, (size_t)P.nrows + 1), "cudaMalloc row_cnt");
@@ -278,6 +294,7 @@ int fp_destroy(fp_handle h) {
     cudaFree(P.d_partials);
     cudaFree(P.d_red);
     cudaFree(P.d_sc);
+    cudaFree(P.d_err);
     cudaFree(P.d_hist);
     cudaFree(P.d_row_ptr);
     cudaFree(P.d_row_cnt);
@@ -296,7 +313,7 @@ int fp_synchronize(fp_handle h) {
     if (!h) return FP_ERR_INVALID;
     Problem& P = h->P;
     FP_CUDA(cudaStreamSynchronize(P.stream), "cudaStreamSynchronize");
-    return FP_OK;
+    return check_device_error(P);
 }
 
 int fp_set_precision(fp_handle h, int precision) {
@@ -351,7 +368,8 @@ int fp_get_green(fp_handle h, double* g6) {
     Problem& P = h->P;
     int rc = ensure_green64(P);
     if (rc) return rc;
-    FP_CUDA(cudaMemcpy(g6, P.d_green64, sizeof(double) * 6 * (size_t)P.nh, cudaMemcpyDeviceToHost),
+    FP_CUDA(cudaMemcpy2D(g6, sizeof(double) * P.nxh, P.d_green64, sizeof(double) * P.rs,
+                         sizeof(double) * P.nxh, 6 * (size_t)P.nrows, cudaMemcpyDeviceToHost),
             "copy");
     return FP_OK;
 }
@@ -393,8 +411,9 @@ int fp_fft_forward(fp_handle h, const double* real_soa, double* half_spectrum) {
     a.precision = fp::kFP64;
     int nparts = 0;
     FP_CUDA(fp::launch_apply(P, a, &nparts), "forward fft");
-    FP_CUDA(cudaMemcpyAsync(half_spectrum, P.d_spec, sizeof(double2) * 3 * (size_t)P.nh,
-                            cudaMemcpyDeviceToHost, P.stream),
+    FP_CUDA(cudaMemcpy2DAsync(half_spectrum, sizeof(double2) * P.nxh, P.d_spec, sizeof(double2) * P.rs,
+                              sizeof(double2) * P.nxh, 3 * (size_t)P.nrows, cudaMemcpyDeviceToHost,
+                              P.stream),
             "copy");
     FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
     return FP_OK;
@@ -405,8 +424,9 @@ int fp_fft_inverse(fp_handle h, const double* half_spectrum, double* real_soa) {
     Problem& P = h->P;
     int rc = alloc_dense(P);
     if (rc) return rc;
-    FP_CUDA(cudaMemcpyAsync(P.d_spec, half_spectrum, sizeof(double2) * 3 * (size_t)P.nh,
-                            cudaMemcpyHostToDevice, P.stream),
+    FP_CUDA(cudaMemcpy2DAsync(P.d_spec, sizeof(double2) * P.rs, half_spectrum, sizeof(double2) * P.nxh,
+                              sizeof(double2) * P.nxh, 3 * (size_t)P.nrows, cudaMemcpyHostToDevice,
+                              P.stream),
             "copy");
     fp::ApplyArgs a;
     a.dst = P.d_dense_out;
@@ -450,7 +470,7 @@ int fp_operator_apply(fp_handle h, const double* x, double* y) {
     if (rc) return rc;
     FP_CUDA(cudaMemcpyAsync(y, P.d_cout, bytes, cudaMemcpyDeviceToHost, P.stream), "copy");
     FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
-    return FP_OK;
+    return check_device_error(P);
 }
 
 int fp_operator_apply_device(fp_handle h, const double* d_x, double* d_y) {

@@ -223,7 +223,10 @@ __device__ __forceinline__ void dft_r(T2 (&v)[R]) {
 // stages
 // ---------------------------------------------------------------------------
 
-enum { kIoSmem = 0, kIoFunc = 1 };
+// Stage input/output modes: shared-memory lines, a functor (global memory),
+// or a functor that reads shared memory the stage's own output overwrites
+// (a barrier separates the loads from the stores).
+enum { kIoSmem = 0, kIoFunc = 1, kIoFuncSmem = 2 };
 
 template <typename T2, int R>
 struct StageRegs {
@@ -335,7 +338,7 @@ __device__ __forceinline__ void fft_stage(T2* const* sl, int n, int ns, int lane
     T2 v[NL][StageRegs<T2, R>::KM][R];
     zero_regs(v);
     stage_load<R, IN, NL>(v, sl, n, lane, tpl, active, src);
-    if (IN == kIoSmem && OUT == kIoSmem) __syncthreads();
+    if ((IN == kIoSmem || IN == kIoFuncSmem) && OUT == kIoSmem) __syncthreads();
     stage_compute<R, S, NL>(v, n, ns, lane, tpl, active, tw);
     stage_store<R, OUT, NL>(v, sl, n, ns, lane, tpl, active, dst);
     if (OUT == kIoSmem) __syncthreads();
@@ -384,7 +387,7 @@ __device__ __forceinline__ void fft_lines(T2* const* sl, const FftPlanDev& p, in
         if (active && lane == 0) {
             for (int l = 0; l < NL; ++l) {
                 T2 v;
-                if constexpr (IN == kIoFunc) v = src(l, 0); else v = sl[l][0];
+                if constexpr (IN != kIoSmem) v = src(l, 0); else v = sl[l][0];
                 if constexpr (OUT == kIoFunc) dst(l, 0, v); else sl[l][0] = v;
             }
         }

@@ -3,6 +3,7 @@
 // (include/fftperm.h).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -47,11 +48,20 @@ struct MinresScalars {
     int pad;
 };
 
+// Cached TMA descriptor of the spectral field for one pass and precision.
+struct TmaCache {
+    bool valid = false;
+    int t = 0;    // kx columns per tile
+    int box = 0;  // rows per box along the transform axis
+    CUtensorMap map;
+};
+
 struct Problem {
     int nx = 0, ny = 0, nz = 0;
     long long n = 0;      // voxels
     int nxh = 0;          // nx/2 + 1
-    long long nh = 0;     // half spectrum points
+    long long rs = 0;     // row stride of spectral fields and Green tables: nxh rounded up to even
+    long long nh = 0;     // half spectrum points stored: rs * ny * nz
     long long nrows = 0;  // ny * nz
     double h = 1.0, mu = 1.0;
     int p_radius = 2;
@@ -100,6 +110,11 @@ struct Problem {
     double* d_hist = nullptr;       // residual history (maxit + 1)
     long long hist_cap = 0;
 
+    // TMA-fed y and z passes: [precision 0 = FP64, 1 = FP32]
+    TmaCache tma_y[2], tma_z[2];
+    bool tma_off = false;      // FFTPERM_NO_TMA=1 selects the register-fed passes
+    int* d_err = nullptr;      // device error flag (a bounded wait gave up)
+
     std::string err;
 };
 
@@ -110,6 +125,7 @@ constexpr int kMaxPartials = 8192;
 // q = 2 pi m / L for m = k + p n, p = -P-1 .. P (nw = 2P + 2 entries per k).
 struct GreenArgs {
     int nx, ny, nz, nxh, nw, pr;
+    long long rs;  // row stride of the table (>= nxh; padding entries are zero)
     double mu;
     const double* sx;  // [nx][nw]
     const double* qx;

@@ -23,6 +23,7 @@
 #include "common.cuh"
 #include "fft_engine.cuh"
 #include "internal.h"
+#include "tma.cuh"
 
 namespace fp {
 
@@ -149,11 +150,12 @@ struct XArgs {
 };
 
 struct YArgs {
-    int ny, nxh, tx, ld;
+    int ny, nxh, tx, ld, nz;
     long long nh, rs;
     FftPlanDev plan;
     void* spec;
     const int* skip;
+    int* err;
 };
 
 struct ZArgs {
@@ -163,6 +165,18 @@ struct ZArgs {
     const void* green;
     void* spec;
     const int* skip;
+    int* err;
+};
+
+// Tiling of a persistent TMA-fed pass.
+struct TmaTile {
+    int ntiles;    // tiles in the pass
+    int ntx;       // kx tiles per line of tiles
+    int t;         // kx columns per tile
+    int nbox;      // TMA boxes along the transform axis
+    int box;       // rows per box
+    int np;        // nbox * box: rows of the raw tile in shared memory
+    int bufbytes;  // bytes of one tile buffer (raw tile or padded lines, larger of the two)
 };
 
 // ---------------------------------------------------------------------------
@@ -173,7 +187,7 @@ template <typename T, int SRC>
 __global__ void __launch_bounds__(256, 3) k_xfwd(XArgs a) {
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     T2* lines = reinterpret_cast<T2*>(smem_raw);
     const int nx = a.nx;
     const int ld = a.ld;
@@ -318,7 +332,7 @@ template <typename T, int S>
 __global__ void __launch_bounds__(256) k_ypass(YArgs a) {
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     T2* lines = reinterpret_cast<T2*>(smem_raw);
     const int tx = a.tx;
     const int k0 = blockIdx.x * tx;
@@ -343,9 +357,9 @@ __global__ void __launch_bounds__(256) k_ypass(YArgs a) {
 // forward's last stage left in this thread's registers.
 // ---------------------------------------------------------------------------
 
-template <int RL, typename T>
-__device__ __forceinline__ void z_fused(const ZArgs& a, c_t<T>* const* sl, ColIo<c_t<T>>& io,
-                                        int c, int lane, bool active) {
+template <int RL, typename T, int IN0, class Src, class Dst>
+__device__ __forceinline__ void z_fused(const ZArgs& a, c_t<T>* const* sl, Src& src, Dst& dst,
+                                        long long gbase, int lane, bool active) {
     using T2 = c_t<T>;
     const FftPlanDev& p = a.plan;
     const T2* tw = plan_tw<T2>(p);
@@ -359,7 +373,7 @@ __device__ __forceinline__ void z_fused(const ZArgs& a, c_t<T>* const* sl, ColIo
     for (int s = 0; s < nst - 1; ++s) {
         const int R = plan_radix<T2>(p, s);
         if (s == 0)
-            fft_stage_rt<-1, kIoFunc, kIoSmem, 3>(R, sl, n, ns, lane, tpl, active, tw, io, ndst);
+            fft_stage_rt<-1, IN0, kIoSmem, 3>(R, sl, n, ns, lane, tpl, active, tw, src, ndst);
         else
             fft_stage_rt<-1, kIoSmem, kIoSmem, 3>(R, sl, n, ns, lane, tpl, active, tw, nsrc, ndst);
         ns *= R;
@@ -369,7 +383,7 @@ __device__ __forceinline__ void z_fused(const ZArgs& a, c_t<T>* const* sl, ColIo
     T2 v[3][KM][RL];
     zero_regs(v);
     if (nst == 1)
-        stage_load<RL, kIoFunc, 3>(v, sl, n, lane, tpl, active, io);
+        stage_load<RL, kIoFunc, 3>(v, sl, n, lane, tpl, active, src);
     else
         stage_load<RL, kIoSmem, 3>(v, sl, n, lane, tpl, active, nsrc);
     stage_compute<RL, -1, 3>(v, n, ns, lane, tpl, active, tw);
@@ -377,14 +391,13 @@ __device__ __forceinline__ void z_fused(const ZArgs& a, c_t<T>* const* sl, ColIo
     const int m = n / RL;
     if (active) {
         const T* g = reinterpret_cast<const T*>(a.green);
-        const long long gb = (long long)blockIdx.y * a.rs + blockIdx.x * a.tz + c;
 #pragma unroll
         for (int kk = 0; kk < KM; ++kk) {
             const int j = lane + kk * tpl;
             if (j < m) {
 #pragma unroll
                 for (int r = 0; r < RL; ++r) {
-                    const long long gi = (long long)(j + r * m) * a.plane + gb;
+                    const long long gi = (long long)(j + r * m) * a.plane + gbase;
                     const T gxx = g[gi], gxy = g[a.gstride + gi], gxz = g[2 * a.gstride + gi];
                     const T gyy = g[3 * a.gstride + gi], gyz = g[4 * a.gstride + gi];
                     const T gzz = g[5 * a.gstride + gi];
@@ -408,7 +421,7 @@ __device__ __forceinline__ void z_fused(const ZArgs& a, c_t<T>* const* sl, ColIo
             for (int r = 0; r < RL; ++r) u[l][kk][r] = v[l][kk][out_slot<RL>(r)];
     stage_compute<RL, +1, 3>(u, n, 1, lane, tpl, active, tw);
     if (nst == 1) {
-        stage_store<RL, kIoFunc, 3>(u, sl, n, 1, lane, tpl, active, io);
+        stage_store<RL, kIoFunc, 3>(u, sl, n, 1, lane, tpl, active, dst);
         return;
     }
     __syncthreads();  // every thread has read its last forward inputs
@@ -418,10 +431,27 @@ __device__ __forceinline__ void z_fused(const ZArgs& a, c_t<T>* const* sl, ColIo
     for (int s = 1; s < nst; ++s) {
         const int R = plan_radix<T2>(p, nst - 1 - s);
         if (s == nst - 1)
-            fft_stage_rt<+1, kIoSmem, kIoFunc, 3>(R, sl, n, ns, lane, tpl, active, tw, nsrc, io);
+            fft_stage_rt<+1, kIoSmem, kIoFunc, 3>(R, sl, n, ns, lane, tpl, active, tw, nsrc, dst);
         else
             fft_stage_rt<+1, kIoSmem, kIoSmem, 3>(R, sl, n, ns, lane, tpl, active, tw, nsrc, ndst);
         ns *= R;
+    }
+}
+
+template <typename T, int IN0, class Src, class Dst>
+__device__ __forceinline__ void z_fused_rt(const ZArgs& a, c_t<T>* const* sl, Src& src, Dst& dst,
+                                           long long gbase, int lane, bool active) {
+    using T2 = c_t<T>;
+    const int nst = plan_nstage<T2>(a.plan);
+    switch (plan_radix<T2>(a.plan, nst - 1)) {
+        case 16:
+            if constexpr (sizeof(T) == 4) z_fused<16, T, IN0>(a, sl, src, dst, gbase, lane, active);
+            break;
+        case 8: z_fused<8, T, IN0>(a, sl, src, dst, gbase, lane, active); break;
+        case 4: z_fused<4, T, IN0>(a, sl, src, dst, gbase, lane, active); break;
+        case 2: z_fused<2, T, IN0>(a, sl, src, dst, gbase, lane, active); break;
+        case 3: z_fused<3, T, IN0>(a, sl, src, dst, gbase, lane, active); break;
+        default: z_fused<5, T, IN0>(a, sl, src, dst, gbase, lane, active); break;
     }
 }
 
@@ -431,7 +461,7 @@ template <typename T, int ZMODE>
 __global__ void __launch_bounds__(256) k_zgreen(ZArgs a) {
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     T2* lines = reinterpret_cast<T2*>(smem_raw);
     const int tz = a.tz;
     const int k0 = blockIdx.x * tz;
@@ -465,16 +495,150 @@ __global__ void __launch_bounds__(256) k_zgreen(ZArgs a) {
             }
             return;
         }
-        switch (plan_radix<T2>(a.plan, nst - 1)) {
-            case 16:
-                if constexpr (sizeof(T) == 4) z_fused<16, T>(a, sl, io, c, lane, active);
-                break;
-            case 8: z_fused<8, T>(a, sl, io, c, lane, active); break;
-            case 4: z_fused<4, T>(a, sl, io, c, lane, active); break;
-            case 2: z_fused<2, T>(a, sl, io, c, lane, active); break;
-            case 3: z_fused<3, T>(a, sl, io, c, lane, active); break;
-            default: z_fused<5, T>(a, sl, io, c, lane, active); break;
+        z_fused_rt<T, kIoFunc>(a, sl, io, io, (long long)blockIdx.y * a.rs + k0 + c, lane, active);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent TMA-fed y and z passes.  One CTA per SM walks its tiles; two
+// shared-memory buffers alternate so that the TMA loads of tile i+1 (three
+// component boxes per tile, completion counted on an mbarrier) run while tile
+// i is transformed.  Stage 0 reads the raw TMA tile, later stages exchange
+// through padded lines in the same buffer, and the last stage writes HBM
+// directly.  Waits are bounded: on a timeout the CTA raises the error flag,
+// drains its own prefetch (bounded too) and returns.
+// ---------------------------------------------------------------------------
+
+template <typename T2>
+struct RawIo {
+    const T2* raw;
+    int np, t, c;
+    __device__ __forceinline__ T2 operator()(int l, int i) const {
+        return raw[((long long)l * np + i) * t + c];
+    }
+};
+
+template <typename T2>
+__device__ __forceinline__ bool tma_pipeline_wait(uint64_t* bars, int i, int b, bool prefetched,
+                                                  int* err) {
+    const bool ok = mbar_wait_bounded(&bars[b], (uint32_t)((i >> 1) & 1));
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) {
+            atomicExch(err, 1);
+            if (prefetched) mbar_wait_bounded(&bars[b ^ 1], (uint32_t)(((i + 1) >> 1) & 1));
         }
+        return false;
+    }
+    return true;
+}
+
+template <typename T, int S>
+__global__ void __launch_bounds__(256) k_ypass_tma(const __grid_constant__ CUtensorMap map, YArgs a,
+                                                   TmaTile tt) {
+    if (a.skip && *a.skip) return;
+    using T2 = c_t<T>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
+    unsigned char* buf0 = smem_raw + 128;
+    const int t = tt.t;
+    const int c = threadIdx.x % t;
+    const int lane = threadIdx.x / t;
+    const uint32_t tile_bytes = (uint32_t)(3 * tt.np * t * sizeof(T2));
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    auto issue = [&](int tile, int b) {
+        const int kx0 = (tile % tt.ntx) * t;
+        const int z = tile / tt.ntx;
+        T2* dst = reinterpret_cast<T2*>(buf0 + (size_t)b * tt.bufbytes);
+        mbar_arrive_expect_tx(&bars[b], tile_bytes);
+        for (int l = 0; l < 3; ++l)
+            for (int yb = 0; yb < tt.nbox; ++yb)
+                tma_load_4d(dst + ((size_t)l * tt.np + (size_t)yb * tt.box) * t, &map, 2 * kx0,
+                            yb * tt.box, z, l, &bars[b]);
+    };
+    int tile = blockIdx.x;
+    if (threadIdx.x == 0 && tile < tt.ntiles) issue(tile, 0);
+    for (int i = 0; tile < tt.ntiles; tile += gridDim.x, ++i) {
+        const int b = i & 1;
+        const int nt = tile + gridDim.x;
+        if (threadIdx.x == 0 && nt < tt.ntiles) {
+            fence_proxy_async_smem();
+            issue(nt, b ^ 1);
+        }
+        if (!tma_pipeline_wait<T2>(bars, i, b, nt < tt.ntiles, a.err)) return;
+        const int kx0 = (tile % tt.ntx) * t;
+        const long long z = tile / tt.ntx;
+        const bool active = (kx0 + c) < a.nxh;
+        T2* buf = reinterpret_cast<T2*>(buf0 + (size_t)b * tt.bufbytes);
+        RawIo<T2> src{buf, tt.np, t, c};
+        ColIo<T2> dst;
+        dst.base = reinterpret_cast<T2*>(a.spec) + z * (long long)a.ny * a.rs + kx0 + (active ? c : 0);
+        dst.cstride = a.nh;
+        dst.estride = a.rs;
+        T2* sl[3];
+#pragma unroll
+        for (int l = 0; l < 3; ++l) sl[l] = buf + (l * t + c) * a.ld;
+        fft_lines<S, kIoFuncSmem, kIoFunc, 3>(sl, a.plan, lane, active, S > 0, src, dst);
+        __syncthreads();  // the buffer is refilled by the prefetch of the next iteration
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_zgreen_tma(const __grid_constant__ CUtensorMap map, ZArgs a,
+                                                    TmaTile tt) {
+    if (a.skip && *a.skip) return;
+    using T2 = c_t<T>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
+    unsigned char* buf0 = smem_raw + 128;
+    const int t = tt.t;
+    const int c = threadIdx.x % t;
+    const int lane = threadIdx.x / t;
+    const uint32_t tile_bytes = (uint32_t)(3 * tt.np * t * sizeof(T2));
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    auto issue = [&](int tile, int b) {
+        const int kx0 = (tile % tt.ntx) * t;
+        const int ky = tile / tt.ntx;
+        T2* dst = reinterpret_cast<T2*>(buf0 + (size_t)b * tt.bufbytes);
+        mbar_arrive_expect_tx(&bars[b], tile_bytes);
+        for (int l = 0; l < 3; ++l)
+            for (int zb = 0; zb < tt.nbox; ++zb)
+                tma_load_4d(dst + ((size_t)l * tt.np + (size_t)zb * tt.box) * t, &map, 2 * kx0, ky,
+                            zb * tt.box, l, &bars[b]);
+    };
+    int tile = blockIdx.x;
+    if (threadIdx.x == 0 && tile < tt.ntiles) issue(tile, 0);
+    for (int i = 0; tile < tt.ntiles; tile += gridDim.x, ++i) {
+        const int b = i & 1;
+        const int nt = tile + gridDim.x;
+        if (threadIdx.x == 0 && nt < tt.ntiles) {
+            fence_proxy_async_smem();
+            issue(nt, b ^ 1);
+        }
+        if (!tma_pipeline_wait<T2>(bars, i, b, nt < tt.ntiles, a.err)) return;
+        const int kx0 = (tile % tt.ntx) * t;
+        const long long ky = tile / tt.ntx;
+        const bool active = (kx0 + c) < a.nxh;
+        T2* buf = reinterpret_cast<T2*>(buf0 + (size_t)b * tt.bufbytes);
+        RawIo<T2> src{buf, tt.np, t, c};
+        ColIo<T2> dst;
+        dst.base = reinterpret_cast<T2*>(a.spec) + ky * a.rs + kx0 + (active ? c : 0);
+        dst.cstride = a.nh;
+        dst.estride = a.plane;
+        T2* sl[3];
+#pragma unroll
+        for (int l = 0; l < 3; ++l) sl[l] = buf + (l * t + c) * a.ld;
+        z_fused_rt<T, kIoFuncSmem>(a, sl, src, dst, ky * a.rs + kx0 + c, lane, active);
+        __syncthreads();
     }
 }
 
@@ -486,7 +650,7 @@ template <typename T, int DST>
 __global__ void __launch_bounds__(256, 3) k_xinv(XArgs a) {
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     T2* lines = reinterpret_cast<T2*>(smem_raw);
     __shared__ double red[4 * 32];
     const int nx = a.nx;
@@ -592,6 +756,81 @@ __global__ void __launch_bounds__(256, 3) k_xinv(XArgs a) {
 // host launcher
 // ---------------------------------------------------------------------------
 
+// ---------------------------------------------------------------------------
+// TMA descriptors
+// ---------------------------------------------------------------------------
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn tma_encoder() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+constexpr int kTmaSmemLimit = 227 * 1024;
+
+// Chooses the tiling of the TMA-fed y (axis 0) or z (axis 1) pass and builds
+// or reuses its descriptor.  Returns false when the TMA path does not apply.
+static bool tma_setup(Problem& P, bool dbl, int axis, int tpl, int ld, TmaTile& tt,
+                      const CUtensorMap** map) {
+    if (P.tma_off || !tma_encoder()) return false;
+    const size_t e = dbl ? sizeof(double) : sizeof(float);
+    const size_t e2 = 2 * e;
+    const int n = axis == 0 ? P.ny : P.nz;
+    if (n < 16) return false;
+    TmaCache& cache = axis == 0 ? P.tma_y[dbl ? 0 : 1] : P.tma_z[dbl ? 0 : 1];
+    tt.nbox = (n + 255) / 256;
+    tt.box = (n + tt.nbox - 1) / tt.nbox;
+    tt.np = tt.nbox * tt.box;
+    int t = P.tile_yz > 0 ? P.tile_yz : (dbl ? 8 : 16);
+    t &= ~1;
+    for (; t >= 2; t /= 2) {
+        if (t * tpl > 256) continue;
+        const size_t raw = (size_t)3 * tt.np * t * e2;
+        const size_t lines = (size_t)3 * t * ld * e2;
+        const size_t buf = ((raw > lines ? raw : lines) + 127) & ~size_t(127);
+        if (128 + 2 * buf > (size_t)kTmaSmemLimit) continue;
+        tt.bufbytes = (int)buf;
+        break;
+    }
+    if (t < 2) return false;
+    tt.t = t;
+    tt.ntx = (P.nxh + t - 1) / t;
+    tt.ntiles = tt.ntx * (axis == 0 ? P.nz : P.ny);
+    if (!cache.valid || cache.t != t || cache.box != tt.box) {
+        const cuuint64_t dims[4] = {(cuuint64_t)(2 * P.nxh), (cuuint64_t)P.ny, (cuuint64_t)P.nz, 3};
+        const cuuint64_t strides[3] = {(cuuint64_t)(2 * P.rs * e), (cuuint64_t)(2 * P.rs * P.ny * e),
+                                       (cuuint64_t)(2 * P.nh * e)};
+        const cuuint32_t box[4] = {(cuuint32_t)(2 * t), axis == 0 ? (cuuint32_t)tt.box : 1u,
+                                   axis == 0 ? 1u : (cuuint32_t)tt.box, 1u};
+        const cuuint32_t estr[4] = {1, 1, 1, 1};
+        const CUresult r = tma_encoder()(
+            &cache.map, dbl ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+            P.d_spec, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return false;
+        cache.valid = true;
+        cache.t = t;
+        cache.box = tt.box;
+    }
+    *map = &cache.map;
+    return true;
+}
+
 static int choose_rows_per_cta(const Problem& P, int tpl, int ld, size_t elem) {
     int rows = 1;
     for (int r = 1; r <= 64; ++r) {
@@ -614,7 +853,7 @@ static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     const int padsh = dbl ? Prec<double2>::PADSH : Prec<float2>::PADSH;
     const int max_yz = 256;  // matches __launch_bounds__ of the y and z passes
     auto tpl_of = [&](const AxisPlan& ap) { return dbl ? ap.dev.tpl64 : ap.dev.tpl32; };
-    const long long rs = P.nxh;
+    const long long rs = P.rs;
     *nparts = 0;
 
     // ---- x passes
@@ -661,6 +900,8 @@ static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     y.plan = P.py.dev;
     y.spec = P.d_spec;
     y.skip = aa.skip;
+    y.err = P.d_err;
+    y.nz = P.nz;
     y.ld = line_stride(P.ny, padsh);
     const int tply = tpl_of(P.py);
     {
@@ -685,6 +926,7 @@ static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     z.green = dbl ? (const void*)P.d_green64 : (const void*)P.d_green32;
     z.spec = P.d_spec;
     z.skip = aa.skip;
+    z.err = P.d_err;
     z.ld = line_stride(P.nz, padsh);
     const int tplz = tpl_of(P.pz);
     {
@@ -695,6 +937,24 @@ static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     const int zthreads = z.tz * tplz;
     const size_t zsmem = (size_t)3 * z.tz * z.ld * elem;
     dim3 zgrid((P.nxh + z.tz - 1) / z.tz, P.ny);
+
+    TmaTile tty{}, ttz{};
+    const CUtensorMap* mapy = nullptr;
+    const CUtensorMap* mapz = nullptr;
+    const bool tma_y = P.d_err && tma_setup(P, dbl, 0, tply, y.ld, tty, &mapy);
+    const bool tma_z = P.d_err && tma_setup(P, dbl, 1, tplz, z.ld, ttz, &mapz);
+    const int ygrid_tma = (int)std::min<long long>(tty.ntiles, P.sm_count);
+    const int zgrid_tma = (int)std::min<long long>(ttz.ntiles, P.sm_count);
+    const size_t ysmem_tma = 128 + 2 * (size_t)tty.bufbytes;
+    const size_t zsmem_tma = 128 + 2 * (size_t)ttz.bufbytes;
+    if (tma_y) y.tx = tty.t;
+    if (tma_z) z.tz = ttz.t;
+
+#define FP_LAUNCH_TMA(kern, grid, threads, smem, map, args, tt)                                  \
+    do {                                                                                          \
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem));     \
+        kern<<<grid, threads, smem, P.stream>>>(*(map), args, tt);                                \
+    } while (0)
 
 #define FP_LAUNCH(kern, grid, threads, smem, args)                                              \
     do {                                                                                          \
@@ -709,22 +969,32 @@ static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
             case kSrcF0: FP_LAUNCH((k_xfwd<T, kSrcF0>), xblocks, xthreads, xsmem, x); break;
             default: FP_LAUNCH((k_xfwd<T, kSrcF0Compact>), xblocks, xthreads, xsmem, x); break;
         }
-        if (P.ny > 1) FP_LAUNCH((k_ypass<T, -1>), ygrid, ythreads, ysmem, y);
+        if (tma_y)
+            FP_LAUNCH_TMA((k_ypass_tma<T, -1>), ygrid_tma, tty.t * tply, ysmem_tma, mapy, y, tty);
+        else if (P.ny > 1)
+            FP_LAUNCH((k_ypass<T, -1>), ygrid, ythreads, ysmem, y);
         if (aa.stage == kStageForward) {
             FP_LAUNCH((k_zgreen<T, 1>), zgrid, zthreads, zsmem, z);
             return cudaGetLastError();
         }
-        FP_LAUNCH((k_zgreen<T, 0>), zgrid, zthreads, zsmem, z);
+        if (tma_z)
+            FP_LAUNCH_TMA((k_zgreen_tma<T>), zgrid_tma, ttz.t * tplz, zsmem_tma, mapz, z, ttz);
+        else
+            FP_LAUNCH((k_zgreen<T, 0>), zgrid, zthreads, zsmem, z);
     } else {
         FP_LAUNCH((k_zgreen<T, 2>), zgrid, zthreads, zsmem, z);
     }
-    if (P.ny > 1) FP_LAUNCH((k_ypass<T, +1>), ygrid, ythreads, ysmem, y);
+    if (tma_y)
+        FP_LAUNCH_TMA((k_ypass_tma<T, +1>), ygrid_tma, tty.t * tply, ysmem_tma, mapy, y, tty);
+    else if (P.ny > 1)
+        FP_LAUNCH((k_ypass<T, +1>), ygrid, ythreads, ysmem, y);
     if (aa.dst_kind == kDstCompact) {
         FP_LAUNCH((k_xinv<T, kDstCompact>), xblocks, xthreads, xsmem, x);
     } else {
         FP_LAUNCH((k_xinv<T, kDstDense>), xblocks, xthreads, xsmem, x);
     }
 #undef FP_LAUNCH
+#undef FP_LAUNCH_TMA
     *nparts = xblocks;
     return cudaGetLastError();
 }

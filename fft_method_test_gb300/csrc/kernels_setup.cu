@@ -174,8 +174,15 @@ cudaError_t launch_support(Problem& P) {
 __global__ void k_green(GreenArgs a) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.nh) return;
-    const int kx = (int)(t % a.nxh);
-    const long long rest = t / a.nxh;
+    const int kx = (int)(t % a.rs);
+    const long long rest = t / a.rs;
+    if (kx >= a.nxh) {  // row padding
+        for (int c = 0; c < 6; ++c) {
+            if (a.g64) a.g64[c * a.nh + t] = 0.0;
+            if (a.g32) a.g32[c * a.nh + t] = 0.0f;
+        }
+        return;
+    }
     const int ky = (int)(rest % a.ny);
     const int kz = (int)(rest / a.ny);
     double s0 = 0, sxx = 0, syy = 0, szz = 0, sxy = 0, sxz = 0, syz = 0;
@@ -285,6 +292,7 @@ cudaError_t launch_green(Problem& P, double* g64, float* g32) {
     a.ny = P.ny;
     a.nz = P.nz;
     a.nxh = P.nxh;
+    a.rs = P.rs;
     a.nw = nw;
     a.pr = Pr;
     a.mu = P.mu;

@@ -10,7 +10,8 @@
 // fields and gets the work queued on its own stream; nothing is allocated.
 //
 // Limits: N = nx*ny*nz <= kNoAllocMaxVoxels (262144, e.g. 64^3),
-// (nx/2+1)*ny*nz <= kNoAllocMaxHalf (135168), ny*nz <= kNoAllocMaxRows (16384),
+// rs*ny*nz <= kNoAllocMaxHalf (139264) with rs = nx/2+1 rounded up to even,
+// ny*nz <= kNoAllocMaxRows (16384),
 // every edge a product of 2, 3 and 5 and <= 640.  Larger grids are rejected
 // with FP_ERR_INVALID; use fp_create / fp_green_apply for them.
 //
@@ -35,7 +36,7 @@ namespace fp {
 namespace {
 
 constexpr long long kNoAllocMaxVoxels = 262144;
-constexpr long long kNoAllocMaxHalf = 135168;
+constexpr long long kNoAllocMaxHalf = 139264;  // 34 * 64 * 64
 constexpr long long kNoAllocMaxRows = 16384;
 constexpr int kNoAllocMaxEdge = 640;
 constexpr int kNoAllocMaxNw = 2 * 8 + 2;  // alias radius P <= 8
@@ -115,7 +116,8 @@ extern "C" int fp_green_apply_noalloc(int nx, int ny, int nz, double voxel_size,
     if (!(mu > 0.0) || !(voxel_size > 0.0)) return FP_ERR_INVALID;
     const long long n = (long long)nx * ny * nz;
     const long long nrows = (long long)ny * nz;
-    const long long nh = (long long)(nx / 2 + 1) * nrows;
+    const long long rs = ((long long)(nx / 2 + 1) + 1) & ~1LL;
+    const long long nh = rs * nrows;
     const int pr = p_radius < 0 ? 0 : p_radius;
     if (n > kNoAllocMaxVoxels || nh > kNoAllocMaxHalf || nrows > kNoAllocMaxRows || nx > kNoAllocMaxEdge ||
         ny > kNoAllocMaxEdge || nz > kNoAllocMaxEdge || 2 * pr + 2 > kNoAllocMaxNw)
@@ -152,11 +154,13 @@ extern "C" int fp_green_apply_noalloc(int nx, int ny, int nz, double voxel_size,
     P.n = n;
     P.nxh = nx / 2 + 1;
     P.nrows = nrows;
+    P.rs = rs;
     P.nh = nh;
     P.h = voxel_size;
     P.mu = mu;
     P.p_radius = pr;
     P.precision = kFP64;
+    P.tma_off = true;  // the register-fed passes: no descriptor or error flag to allocate
     P.stream = s;
     P.d_spec = sb + kOffSpec;
     P.d_green64 = reinterpret_cast<double*>(sb + kOffGreen);
@@ -167,6 +171,7 @@ extern "C" int fp_green_apply_noalloc(int nx, int ny, int nz, double voxel_size,
     g.ny = ny;
     g.nz = nz;
     g.nxh = P.nxh;
+    g.rs = rs;
     g.nw = 2 * pr + 2;
     g.pr = pr;
     g.mu = mu;

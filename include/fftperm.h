@@ -137,8 +137,9 @@ int fp_solve_permeability(fp_handle h, double tol, int64_t maxit, double K[9],
  * SoA) and a cudaStream_t (NULL = the legacy default stream); the work is
  * queued on that stream and the call returns without waiting.  FP64.
  * All working memory is one fixed, file-scope device array of about 14 MB,
- * so the grid is limited to N <= 262144 voxels (e.g. 64^3), (nx/2+1)*ny*nz <=
- * 135168 and ny*nz <= 16384; larger grids return FP_ERR_INVALID.  The array is
+ * so the grid is limited to N <= 262144 voxels (e.g. 64^3), rs*ny*nz <=
+ * 139264 (rs = nx/2+1 rounded up to even) and ny*nz <= 16384; larger grids
+ * return FP_ERR_INVALID.  The array is
  * shared by all calls: calls that overlap on the GPU race and must be
  * serialised by the caller.  The first call on a device resolves the array's
  * address; make that first call before any stream capture. */
