@@ -86,20 +86,39 @@ __global__ void k_alpha(MinresScalars* sc, const double* __restrict__ partials, 
     }
 }
 
+// Two voxels (six doubles, three aligned double2) per thread: components are
+// static, loads are 16-byte vectors.  The odd tail voxel is handled by the
+// first thread of block 0.
 __global__ void k_zupd(const MinresScalars* sc, double* __restrict__ z, const double* __restrict__ v,
-                       const double* __restrict__ v_old, long long m, double* partials) {
+                       const double* __restrict__ v_old, long long nb, double* partials) {
     if (sc->done) return;
     __shared__ double red[32];
     const double alpha = sc->alpha, beta = sc->beta;
-    const double mz0 = sc->zmean[0], mz1 = sc->zmean[1], mz2 = sc->zmean[2];
+    const double mz[3] = {sc->zmean[0], sc->zmean[1], sc->zmean[2]};
     double acc[1] = {0.0};
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % 3);
-        const double mz = c == 0 ? mz0 : (c == 1 ? mz1 : mz2);
-        const double zi = (z[i] - mz) - (alpha * v[i] + beta * v_old[i]);
-        z[i] = zi;
-        acc[0] += zi * zi;
+    const long long npair = nb >> 1;
+    double2* z2 = reinterpret_cast<double2*>(z);
+    const double2* v2 = reinterpret_cast<const double2*>(v);
+    const double2* o2 = reinterpret_cast<const double2*>(v_old);
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < npair;
+         k += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int h = 0; h < 3; ++h) {
+            const double2 zz = z2[3 * k + h], vv = v2[3 * k + h], oo = o2[3 * k + h];
+            const int c0 = (2 * h) % 3, c1 = (2 * h + 1) % 3;
+            const double a0 = (zz.x - mz[c0]) - (alpha * vv.x + beta * oo.x);
+            const double a1 = (zz.y - mz[c1]) - (alpha * vv.y + beta * oo.y);
+            z2[3 * k + h] = make_double2(a0, a1);
+            acc[0] += a0 * a0 + a1 * a1;
+        }
+    }
+    if ((nb & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+        for (int c = 0; c < 3; ++c) {
+            const long long i = 3 * (nb - 1) + c;
+            const double a0 = (z[i] - mz[c]) - (alpha * v[i] + beta * v_old[i]);
+            z[i] = a0;
+            acc[0] += a0 * a0;
+        }
     }
     double o[1];
     block_sum<1>(acc, red, o);
@@ -157,7 +176,7 @@ __global__ void k_scalar(MinresScalars* sc, const double* __restrict__ partials,
 
 __global__ void k_vwupd(const MinresScalars* sc, const double* __restrict__ z, const double* __restrict__ v,
                         double* __restrict__ v_new, double* __restrict__ w_prev_to_next,
-                        const double* __restrict__ w, double* __restrict__ x, long long m,
+                        const double* __restrict__ w, double* __restrict__ x, long long nb,
                         double* partials) {
     if (sc->done) return;
     __shared__ double red[4 * 32];
@@ -166,15 +185,41 @@ __global__ void k_vwupd(const MinresScalars* sc, const double* __restrict__ z, c
     const bool vb = beta_new > kBreakdownEps;
     const bool rb = rho > kBreakdownEps;
     double acc[4] = {0, 0, 0, 0};
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
-         i += (long long)gridDim.x * blockDim.x) {
-        const double vo = v[i];  // becomes v_old
-        const double vn = vb ? z[i] / beta_new : 0.0;
-        v_new[i] = vn;
-        const double wn = rb ? (vo - eps * w_prev_to_next[i] - delta * w[i]) / rho : 0.0;
-        w_prev_to_next[i] = wn;
-        x[i] += step * wn;
-        acc[(int)(i % 3)] += vn;
+    const long long npair = nb >> 1;
+    const double2* z2 = reinterpret_cast<const double2*>(z);
+    const double2* v2 = reinterpret_cast<const double2*>(v);
+    double2* vn2 = reinterpret_cast<double2*>(v_new);
+    double2* wp2 = reinterpret_cast<double2*>(w_prev_to_next);
+    const double2* w2 = reinterpret_cast<const double2*>(w);
+    double2* x2 = reinterpret_cast<double2*>(x);
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < npair;
+         k += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int h = 0; h < 3; ++h) {
+            const long long q = 3 * k + h;
+            const double2 zz = z2[q], vo = v2[q], wp = wp2[q], ww = w2[q], xx = x2[q];
+            const double vn0 = vb ? zz.x / beta_new : 0.0;
+            const double vn1 = vb ? zz.y / beta_new : 0.0;
+            const double wn0 = rb ? (vo.x - eps * wp.x - delta * ww.x) / rho : 0.0;
+            const double wn1 = rb ? (vo.y - eps * wp.y - delta * ww.y) / rho : 0.0;
+            vn2[q] = make_double2(vn0, vn1);
+            wp2[q] = make_double2(wn0, wn1);
+            x2[q] = make_double2(xx.x + step * wn0, xx.y + step * wn1);
+            acc[(2 * h) % 3] += vn0;
+            acc[(2 * h + 1) % 3] += vn1;
+        }
+    }
+    if ((nb & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+        for (int c = 0; c < 3; ++c) {
+            const long long i = 3 * (nb - 1) + c;
+            const double vo = v[i];
+            const double vn = vb ? z[i] / beta_new : 0.0;
+            v_new[i] = vn;
+            const double wn = rb ? (vo - eps * w_prev_to_next[i] - delta * w[i]) / rho : 0.0;
+            w_prev_to_next[i] = wn;
+            x[i] += step * wn;
+            acc[c] += vn;
+        }
     }
     double o[4];
     block_sum<4>(acc, red, o);
@@ -364,7 +409,6 @@ cudaError_t minres_start(Problem& P, const double* b, const double* x0, double t
 }
 
 cudaError_t minres_iteration(Problem& P) {
-    const long long m = 3 * P.nb;
     const long long k = g_queued++;
     double* v = P.d_v[k % 3];
     double* v_old = P.d_v[(k + 2) % 3];
@@ -384,10 +428,10 @@ cudaError_t minres_iteration(Problem& P) {
     if (e != cudaSuccess) return e;
     const double inv_nb = 1.0 / (double)P.nb;
     k_alpha<<<1, 512, 0, P.stream>>>(P.d_sc, P.d_partials, nparts, inv_nb);
-    const int blocks = vec_blocks(P, m);
-    k_zupd<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, P.d_z, v, v_old, m, P.d_partials);
+    const int blocks = vec_blocks(P, (P.nb + 1) / 2);
+    k_zupd<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, P.d_z, v, v_old, P.nb, P.d_partials);
     k_scalar<<<1, 256, 0, P.stream>>>(P.d_sc, P.d_partials, blocks, P.d_hist);
-    k_vwupd<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, P.d_z, v, v_new, w_prev, w, P.d_x, m,
+    k_vwupd<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, P.d_z, v, v_new, w_prev, w, P.d_x, P.nb,
                                                    P.d_partials);
     k_finish<<<1, 256, 0, P.stream>>>(P.d_sc, P.d_partials, blocks);
     return cudaGetLastError();
