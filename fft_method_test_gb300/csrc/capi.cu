@@ -137,8 +137,29 @@ int device_build_rhs(Problem& P, const double g[3], double* d_b) {
     return FP_OK;
 }
 
-// MINRES on device vectors; d_x receives the solution (P.d_x is used as the
-// iterate).  hist_host may be null.
+// True relative residual |b - A x| / |b| with the current apply precision.
+int true_residual(Problem& P, const double* d_b, double rhs_norm, double* rel) {
+    int rc = device_operator_apply(P, P.d_x, P.d_cout);
+    if (rc) return rc;
+    FP_CUDA(fp::launch_resnorm(P, d_b, P.d_cout, P.d_red + 12), "resnorm");
+    double h[4];
+    FP_CUDA(cudaMemcpyAsync(h, P.d_red + 12, sizeof(double) * 4, cudaMemcpyDeviceToHost, P.stream),
+            "copy");
+    FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+    *rel = std::sqrt(h[3] > 0.0 ? h[3] : 0.0) / rhs_norm;
+    return FP_OK;
+}
+
+// MINRES on device vectors (src/solver/MinresSolver.cpp:46-218); P.d_x
+// receives the solution.  hist_host may be null.
+//
+// FP64 mode runs the reference's recurrence unchanged.  Mixed mode (FP32
+// operator applies, FP64 Lanczos vectors and scalars) adds reliable updates:
+// every P.reliable_interval iterations the true residual |b - A x| is
+// recomputed; the solve stops on the true residual, and when the recurrence
+// estimate has run ahead of it (the FP32 apply's accuracy floor) MINRES is
+// restarted from the current iterate.  The history then holds the last
+// restart's segment.
 int device_minres(Problem& P, const double* d_b, const double* d_x0, double tol, long long maxit,
                   double* hist_host, fp_solver_stats* st) {
     if (!(tol > 0.0)) return fail(P, FP_ERR_INVALID, "MinresSolver tolerance must be positive");
@@ -148,18 +169,51 @@ int device_minres(Problem& P, const double* d_b, const double* d_x0, double tol,
         FP_CUDA(dalloc(&P.d_hist, (size_t)maxit + 1), "cudaMalloc hist");
         P.hist_cap = maxit + 1;
     }
+    const bool reliable = P.precision == fp::kMixed && P.reliable_interval > 0;
     FP_CUDA(fp::minres_start(P, d_b, d_x0, tol, maxit), "minres_start");
     FP_CUDA(cudaMemcpyAsync(P.h_sc, P.d_sc, sizeof(fp::MinresScalars), cudaMemcpyDeviceToHost,
                             P.stream),
             "copy");
     FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
-    const int chunk = 16;
-    while (!P.h_sc->done) {
-        for (int i = 0; i < chunk; ++i) FP_CUDA(fp::minres_iteration(P), "minres_iteration");
-        FP_CUDA(cudaMemcpyAsync(P.h_sc, P.d_sc, sizeof(fp::MinresScalars), cudaMemcpyDeviceToHost,
-                                P.stream),
-                "copy");
-        FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+    const int chunk = reliable ? P.reliable_interval : 16;
+    long long done_its = 0;  // iterations of finished restart segments
+    int restarts = 0;
+    double true_rel = -1.0;
+    const int max_restarts = 20;
+    for (;;) {
+        if (!P.h_sc->done) {
+            for (int i = 0; i < chunk; ++i) FP_CUDA(fp::minres_iteration(P), "minres_iteration");
+            FP_CUDA(cudaMemcpyAsync(P.h_sc, P.d_sc, sizeof(fp::MinresScalars),
+                                    cudaMemcpyDeviceToHost, P.stream),
+                    "copy");
+            FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+        }
+        if (!reliable) {
+            if (P.h_sc->done) break;
+            continue;
+        }
+        const fp::MinresScalars s = *P.h_sc;
+        const long long total = done_its + s.it;
+        int rc = true_residual(P, d_b, s.rhs_norm, &true_rel);
+        if (rc) return rc;
+        if (true_rel <= tol) break;
+        const bool ahead = s.rel_res < 0.25 * true_rel || s.converged || s.breakdown == 2;
+        if (total >= maxit || restarts >= max_restarts) break;
+        if (ahead) {
+            // restart from the current iterate with the remaining budget
+            FP_CUDA(cudaMemcpyAsync(P.d_cin, P.d_x, sizeof(double) * 3 * (size_t)P.nb,
+                                    cudaMemcpyDeviceToDevice, P.stream),
+                    "copy");
+            done_its = total;
+            ++restarts;
+            FP_CUDA(fp::minres_start(P, d_b, P.d_cin, tol, maxit - total), "minres_start");
+            FP_CUDA(cudaMemcpyAsync(P.h_sc, P.d_sc, sizeof(fp::MinresScalars),
+                                    cudaMemcpyDeviceToHost, P.stream),
+                    "copy");
+            FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+        } else if (s.done) {
+            break;
+        }
     }
     const fp::MinresScalars s = *P.h_sc;
     {
@@ -172,10 +226,15 @@ int device_minres(Problem& P, const double* d_b, const double* d_x0, double tol,
                 "hist copy");
     }
     if (st) {
-        st->iterations = s.it;
-        st->final_rel_residual = s.rel_res;
-        st->converged = s.converged ? 1 : (s.rel_res <= tol ? 1 : 0);
-        st->refinements = 0;
+        st->iterations = done_its + s.it;
+        if (reliable) {
+            st->final_rel_residual = true_rel;
+            st->converged = true_rel <= tol ? 1 : 0;
+        } else {
+            st->final_rel_residual = s.rel_res;
+            st->converged = s.converged ? 1 : (s.rel_res <= tol ? 1 : 0);
+        }
+        st->refinements = restarts;
     }
     return FP_OK;
 }

@@ -69,6 +69,7 @@ struct Problem {
     cudaStream_t stream = nullptr;
     int sm_count = 0;
     int tile_yz = 0;  // kx columns per CTA of the y and z passes (0 = default)
+    int reliable_interval = 20;  // mixed precision: true-residual check every this many iterations
 
     AxisPlan px, py, pz;
 
@@ -194,6 +195,8 @@ cudaError_t minres_start(Problem& P, const double* b, const double* x0, double t
                          long long maxit);
 cudaError_t minres_iteration(Problem& P);
 cudaError_t launch_sub_mean(Problem& P, double* v, const double* sums, double scale);
+// out4[3] = |b - ax|^2
+cudaError_t launch_resnorm(Problem& P, const double* b, const double* ax, double* out4);
 cudaError_t launch_gather_sum(Problem& P, const double* u_dense, double* out4);
 cudaError_t launch_add_const3(Problem& P, double* u_dense, const double* add3);
 cudaError_t launch_background_force(Problem& P, const double cf[3], const double cs[3],

@@ -514,6 +514,30 @@ __global__ void k_background_force_support(const int* __restrict__ support, long
 
 }  // namespace
 
+// sum of (b - ax)^2 over the compact vectors, [blocks][4] partials with the sum in slot 3
+__global__ void k_resnorm(const double* __restrict__ b, const double* __restrict__ ax, long long m,
+                          double* partials) {
+    __shared__ double red[4 * 32];
+    double acc[4] = {0, 0, 0, 0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double r = b[i] - ax[i];
+        acc[3] += r * r;
+    }
+    double o[4];
+    block_sum<4>(acc, red, o);
+    if (threadIdx.x == 0)
+        for (int j = 0; j < 4; ++j) partials[4LL * blockIdx.x + j] = o[j];
+}
+
+cudaError_t launch_resnorm(Problem& P, const double* b, const double* ax, double* out4) {
+    const long long m = 3 * P.nb;
+    const int blocks = vec_blocks(P, m);
+    k_resnorm<<<blocks, kVecThreads, 0, P.stream>>>(b, ax, m, P.d_partials);
+    k_reduce4<<<1, 512, 0, P.stream>>>(P.d_partials, blocks, out4);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_sub_mean(Problem& P, double* v, const double* sums, double scale) {
     const long long m = 3 * P.nb;
     k_sub_mean<<<vec_blocks(P, m), kVecThreads, 0, P.stream>>>(
