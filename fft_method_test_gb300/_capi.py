@@ -36,6 +36,7 @@ EXPORTED = [
     "fp_operator_apply", "fp_operator_apply_device", "fp_build_rhs", "fp_minres", "fp_recover",
     "fp_solve_load_case", "fp_solve_permeability", "fp_brinkman_solve",
     "fp_brinkman_permeability", "fp_brinkman_last_error", "fp_green_apply_noalloc",
+    "fp_kernel_launch_count", "fp_brinkman_fft_solve", "fp_brinkman_fft_permeability",
 ]
 
 
@@ -83,6 +84,7 @@ _SIGNATURES = {
     "fp_last_error": ([_h], C.c_char_p),
     "fp_stream": ([_h], C.c_void_p),
     "fp_synchronize": ([_h], C.c_int),
+    "fp_kernel_launch_count": ([], C.c_longlong),
     "fp_set_precision": ([_h, C.c_int], C.c_int),
     "fp_set_geometry": ([_h, _u8p, C.c_int, C.POINTER(C.c_int64)], C.c_int),
     "fp_get_support": ([_h, _i64p], C.c_int),
@@ -107,6 +109,12 @@ _SIGNATURES = {
                                   C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
                                   C.c_double, _dp, C.POINTER(BrinkmanStats)], C.c_int),
     "fp_brinkman_last_error": ([], C.c_char_p),
+    "fp_brinkman_fft_solve": ([C.c_int, C.c_int, C.c_int, _u32p, C.c_uint32, C.c_double,
+                               C.c_double, C.c_double, C.c_int, _dp, C.c_void_p, C.c_void_p,
+                               C.c_void_p, C.c_void_p, _dp, C.POINTER(BrinkmanStats)], C.c_int),
+    "fp_brinkman_fft_permeability": ([C.c_int, C.c_int, C.c_int, _u32p, C.c_uint32, C.c_double,
+                                      C.c_double, C.c_double, C.c_int, C.c_double, C.c_double,
+                                      _dp, C.POINTER(BrinkmanStats)], C.c_int),
     "fp_green_apply_noalloc": ([C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
                                 C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
 }

@@ -18,9 +18,7 @@
 #include "../../include/fftperm.h"
 #include "internal.h"
 
-struct fp_problem {
-    fp::Problem P;
-};
+std::atomic<long long> fp::g_kernel_launches{0};
 
 namespace {
 
@@ -54,6 +52,9 @@ void free_geometry(Problem& P) {
     cudaFree(P.d_b);
     cudaFree(P.d_x);
     cudaFree(P.d_z);
+    cudaFree(P.d_r0);
+    cudaFree(P.d_corr);
+    P.d_r0 = P.d_corr = nullptr;
     for (auto& v : P.d_v) cudaFree(v), v = nullptr;
     for (auto& w : P.d_w) cudaFree(w), w = nullptr;
     P.d_support = nullptr;
@@ -98,6 +99,18 @@ int ensure_green64(Problem& P) {
     return FP_OK;
 }
 
+// Mixed mode needs both tables: FP32 for the Krylov applies, FP64 for the
+// residuals that start and end each refinement segment.  One launch fills both.
+int ensure_green_both(Problem& P) {
+    if (P.d_green32 && P.d_green64) return FP_OK;
+    if (P.d_green32) return ensure_green64(P);
+    if (P.d_green64) return ensure_green32(P);
+    FP_CUDA(dalloc(&P.d_green64, 6 * (size_t)P.nh), "cudaMalloc green64");
+    FP_CUDA(dalloc(&P.d_green32, 6 * (size_t)P.nh), "cudaMalloc green32");
+    FP_CUDA(fp::launch_green(P, P.d_green64, P.d_green32), "green precompute");
+    return FP_OK;
+}
+
 // y = P_B A_raw P_B x on device compact vectors (src/bignonnet/VariationalOperator.cpp:19-41)
 int device_operator_apply(Problem& P, const double* d_x, double* d_y) {
     FP_CUDA(fp::launch_sum3(P, d_x, P.nb, P.d_red), "sum");
@@ -137,10 +150,21 @@ int device_build_rhs(Problem& P, const double g[3], double* d_b) {
     return FP_OK;
 }
 
-// True relative residual |b - A x| / |b| with the current apply precision.
-int true_residual(Problem& P, const double* d_b, double rhs_norm, double* rel) {
-    int rc = device_operator_apply(P, P.d_x, P.d_cout);
-    if (rc) return rc;
+// |b - A y| / rhs_norm, A applied at the given precision (kFP64 / kMixed).
+int residual_norm(Problem& P, const double* d_b, const double* d_y, int precision, double rhs_norm,
+                  double* rel) {
+    FP_CUDA(fp::launch_sum3(P, d_y, P.nb, P.d_red), "sum");
+    fp::ApplyArgs a;
+    a.src = d_y;
+    a.src_sum = P.d_red;
+    a.dst = P.d_cout;
+    a.src_kind = fp::kSrcCompact;
+    a.dst_kind = fp::kDstCompact;
+    a.precision = precision;
+    int nparts = 0;
+    FP_CUDA(fp::launch_apply(P, a, &nparts), "apply");
+    FP_CUDA(fp::launch_reduce4(P, nparts, P.d_red + 4), "reduce");
+    FP_CUDA(fp::launch_sub_mean(P, P.d_cout, P.d_red + 4, 1.0), "sub_mean");
     FP_CUDA(fp::launch_resnorm(P, d_b, P.d_cout, P.d_red + 12), "resnorm");
     double h[4];
     FP_CUDA(cudaMemcpyAsync(h, P.d_red + 12, sizeof(double) * 4, cudaMemcpyDeviceToHost, P.stream),
@@ -150,16 +174,30 @@ int true_residual(Problem& P, const double* d_b, double rhs_norm, double* rel) {
     return FP_OK;
 }
 
+int read_scalars(Problem& P) {
+    FP_CUDA(cudaMemcpyAsync(P.h_sc, P.d_sc, sizeof(fp::MinresScalars), cudaMemcpyDeviceToHost,
+                            P.stream),
+            "copy");
+    FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+    return FP_OK;
+}
+
 // MINRES on device vectors (src/solver/MinresSolver.cpp:46-218); P.d_x
 // receives the solution.  hist_host may be null.
 //
-// FP64 mode runs the reference's recurrence unchanged.  Mixed mode (FP32
-// operator applies, FP64 Lanczos vectors and scalars) adds reliable updates:
-// every P.reliable_interval iterations the true residual |b - A x| is
-// recomputed; the solve stops on the true residual, and when the recurrence
-// estimate has run ahead of it (the FP32 apply's accuracy floor) MINRES is
-// restarted from the current iterate.  The history then holds the last
-// restart's segment.
+// FP64 mode runs the reference's recurrence unchanged.
+//
+// Mixed mode (FP32 operator applies, FP64 Lanczos vectors and scalars) is
+// MINRES inside mixed-precision iterative refinement.  Each segment starts
+// from the current iterate x0 with the residual r0 = b - A x0 computed with
+// the FP64 operator, and runs the reference recurrence on the FP32 operator.
+// Every P.reliable_interval iterations the segment's own true residual
+// |r0 - A32 (x - x0)| is recomputed (reliable update).  A segment ends when
+// the recurrence reports convergence or breakdown, when that true residual is
+// below tol, or when the recurrence estimate has run ahead of it (below a
+// quarter of it).  The FP64 residual |b - A x| then decides: below tol the
+// solve has converged, otherwise a new segment starts from x.  The reported
+// residual is that FP64 residual; the history holds the last segment.
 int device_minres(Problem& P, const double* d_b, const double* d_x0, double tol, long long maxit,
                   double* hist_host, fp_solver_stats* st) {
     if (!(tol > 0.0)) return fail(P, FP_ERR_INVALID, "MinresSolver tolerance must be positive");
@@ -169,51 +207,74 @@ int device_minres(Problem& P, const double* d_b, const double* d_x0, double tol,
         FP_CUDA(dalloc(&P.d_hist, (size_t)maxit + 1), "cudaMalloc hist");
         P.hist_cap = maxit + 1;
     }
-    const bool reliable = P.precision == fp::kMixed && P.reliable_interval > 0;
-    FP_CUDA(fp::minres_start(P, d_b, d_x0, tol, maxit), "minres_start");
-    FP_CUDA(cudaMemcpyAsync(P.h_sc, P.d_sc, sizeof(fp::MinresScalars), cudaMemcpyDeviceToHost,
-                            P.stream),
-            "copy");
-    FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
-    const int chunk = reliable ? P.reliable_interval : 16;
-    long long done_its = 0;  // iterations of finished restart segments
+    const bool mixed = P.precision == fp::kMixed && P.reliable_interval > 0;
+    if (mixed) {
+        int rc = ensure_green_both(P);
+        if (rc) return rc;
+    }
+    const size_t bytes = sizeof(double) * 3 * (size_t)P.nb;
+    // the first segment's r0 uses the FP64 operator in mixed mode
+    FP_CUDA(fp::minres_start(P, d_b, d_x0, tol, maxit, mixed ? fp::kFP64 : -1), "minres_start");
+    const double* seg_x0 = d_x0;  // null: the segment starts from zero
+    if (mixed) {
+        FP_CUDA(cudaMemcpyAsync(P.d_r0, P.d_z, bytes, cudaMemcpyDeviceToDevice, P.stream), "copy");
+        if (d_x0) {
+            FP_CUDA(cudaMemcpyAsync(P.d_corr, d_x0, bytes, cudaMemcpyDeviceToDevice, P.stream),
+                    "copy");
+            seg_x0 = P.d_corr;  // keep the start point (d_x0 may alias P.d_cin)
+        }
+    }
+    {
+        int rc = read_scalars(P);
+        if (rc) return rc;
+    }
+    const int chunk = mixed ? P.reliable_interval : 16;
+    long long done_its = 0;  // iterations of finished segments
     int restarts = 0;
-    double true_rel = -1.0;
+    double rel64 = -1.0;
+    bool converged64 = false;
     const int max_restarts = 20;
     for (;;) {
         if (!P.h_sc->done) {
             for (int i = 0; i < chunk; ++i) FP_CUDA(fp::minres_iteration(P), "minres_iteration");
-            FP_CUDA(cudaMemcpyAsync(P.h_sc, P.d_sc, sizeof(fp::MinresScalars),
-                                    cudaMemcpyDeviceToHost, P.stream),
-                    "copy");
-            FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+            int rc = read_scalars(P);
+            if (rc) return rc;
         }
-        if (!reliable) {
+        if (!mixed) {
             if (P.h_sc->done) break;
             continue;
         }
         const fp::MinresScalars s = *P.h_sc;
         const long long total = done_its + s.it;
-        int rc = true_residual(P, d_b, s.rhs_norm, &true_rel);
+        // the segment's true residual |r0 - A32 (x - x0)| / |b|
+        double seg_rel = 0.0;
+        if (!s.done || !s.converged) {
+            const double* y = P.d_x;
+            if (seg_x0) {
+                FP_CUDA(fp::launch_axpby(P, P.d_cin, 1.0, P.d_x, -1.0, seg_x0), "diff");
+                y = P.d_cin;
+            }
+            int rc = residual_norm(P, P.d_r0, y, fp::kMixed, s.rhs_norm, &seg_rel);
+            if (rc) return rc;
+        }
+        const bool seg_end = s.done || seg_rel <= tol || s.rel_res < 0.25 * seg_rel;
+        if (!seg_end) continue;
+        int rc = residual_norm(P, d_b, P.d_x, fp::kFP64, s.rhs_norm, &rel64);
         if (rc) return rc;
-        if (true_rel <= tol) break;
-        const bool ahead = s.rel_res < 0.25 * true_rel || s.converged || s.breakdown == 2;
-        if (total >= maxit || restarts >= max_restarts) break;
-        if (ahead) {
-            // restart from the current iterate with the remaining budget
-            FP_CUDA(cudaMemcpyAsync(P.d_cin, P.d_x, sizeof(double) * 3 * (size_t)P.nb,
-                                    cudaMemcpyDeviceToDevice, P.stream),
-                    "copy");
-            done_its = total;
-            ++restarts;
-            FP_CUDA(fp::minres_start(P, d_b, P.d_cin, tol, maxit - total), "minres_start");
-            FP_CUDA(cudaMemcpyAsync(P.h_sc, P.d_sc, sizeof(fp::MinresScalars),
-                                    cudaMemcpyDeviceToHost, P.stream),
-                    "copy");
-            FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
-        } else if (s.done) {
+        if (rel64 <= tol) {
+            converged64 = true;
             break;
         }
+        if (total >= maxit || restarts >= max_restarts) break;
+        // next segment from the current iterate, r0 with the FP64 operator
+        FP_CUDA(cudaMemcpyAsync(P.d_corr, P.d_x, bytes, cudaMemcpyDeviceToDevice, P.stream), "copy");
+        seg_x0 = P.d_corr;
+        done_its = total;
+        ++restarts;
+        FP_CUDA(fp::minres_start(P, d_b, P.d_corr, tol, maxit - total, fp::kFP64), "minres_start");
+        FP_CUDA(cudaMemcpyAsync(P.d_r0, P.d_z, bytes, cudaMemcpyDeviceToDevice, P.stream), "copy");
+        rc = read_scalars(P);
+        if (rc) return rc;
     }
     const fp::MinresScalars s = *P.h_sc;
     {
@@ -227,9 +288,9 @@ int device_minres(Problem& P, const double* d_b, const double* d_x0, double tol,
     }
     if (st) {
         st->iterations = done_its + s.it;
-        if (reliable) {
-            st->final_rel_residual = true_rel;
-            st->converged = true_rel <= tol ? 1 : 0;
+        if (mixed) {
+            st->final_rel_residual = rel64;
+            st->converged = converged64 ? 1 : 0;
         } else {
             st->final_rel_residual = s.rel_res;
             st->converged = s.converged ? 1 : (s.rel_res <= tol ? 1 : 0);
@@ -286,6 +347,13 @@ extern "C" {
 
 int fp_create(int nx, int ny, int nz, double voxel_size, double mu, int p_radius, int precision,
               fp_handle* out) {
+    return fp::create_handle(nx, ny, nz, voxel_size, mu, p_radius, precision, true, out);
+}
+
+}  // extern "C"
+
+int fp::create_handle(int nx, int ny, int nz, double voxel_size, double mu, int p_radius,
+                      int precision, bool with_green, fp_handle* out) {
     if (!out) return FP_ERR_INVALID;
     *out = nullptr;
     fp_problem* h = new (std::nothrow) fp_problem();
@@ -332,10 +400,13 @@ int fp_create(int nx, int ny, int nz, double voxel_size, double mu, int p_radius
     FP_CUDA(dalloc(&P.d_row_ptr, (size_t)P.nrows + 1), "cudaMalloc row_ptr");
     FP_CUDA(dalloc(&P.d_row_cnt, (size_t)P.nrows + 1), "cudaMalloc row_cnt");
     FP_CUDA(dalloc(&P.d_mask, (size_t)P.n), "cudaMalloc mask");
-    int rc = (precision == FP_PREC_MIXED) ? ensure_green32(P) : ensure_green64(P);
+    if (!with_green) return FP_OK;
+    int rc = (precision == FP_PREC_MIXED) ? ensure_green_both(P) : ensure_green64(P);
     if (rc) return rc;
     return FP_OK;
 }
+
+extern "C" {
 
 int fp_destroy(fp_handle h) {
     if (!h) return FP_OK;
@@ -368,6 +439,10 @@ const char* fp_last_error(fp_handle h) { return h ? h->P.err.c_str() : "null han
 
 void* fp_stream(fp_handle h) { return h ? (void*)h->P.stream : nullptr; }
 
+long long fp_kernel_launch_count(void) {
+    return fp::g_kernel_launches.load(std::memory_order_relaxed);
+}
+
 int fp_synchronize(fp_handle h) {
     if (!h) return FP_ERR_INVALID;
     Problem& P = h->P;
@@ -380,7 +455,7 @@ int fp_set_precision(fp_handle h, int precision) {
     Problem& P = h->P;
     if (precision != FP_PREC_FP64 && precision != FP_PREC_MIXED)
         return fail(P, FP_ERR_INVALID, "unknown precision mode");
-    int rc = (precision == FP_PREC_MIXED) ? ensure_green32(P) : ensure_green64(P);
+    int rc = (precision == FP_PREC_MIXED) ? ensure_green_both(P) : ensure_green64(P);
     if (rc) return rc;
     P.precision = precision;
     return FP_OK;
@@ -403,6 +478,8 @@ int fp_set_geometry(fp_handle h, const uint8_t* fluid_mask, int support_mode, in
     FP_CUDA(dalloc(&P.d_b, m), "cudaMalloc");
     FP_CUDA(dalloc(&P.d_x, m), "cudaMalloc");
     FP_CUDA(dalloc(&P.d_z, m), "cudaMalloc");
+    FP_CUDA(dalloc(&P.d_r0, m), "cudaMalloc");
+    FP_CUDA(dalloc(&P.d_corr, m), "cudaMalloc");
     for (auto& v : P.d_v) FP_CUDA(dalloc(&v, m), "cudaMalloc");
     for (auto& w : P.d_w) FP_CUDA(dalloc(&w, m), "cudaMalloc");
     FP_CUDA(cudaStreamSynchronize(P.stream), "sync");

@@ -4,7 +4,15 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 namespace fp {
+
+// Process-wide count of this library's kernel launches (all devices and
+// streams), read by fp_kernel_launch_count.  Every launch site bumps it.
+extern std::atomic<long long> g_kernel_launches;
+#define FP_LAUNCHED() (::fp::g_kernel_launches.fetch_add(1, std::memory_order_relaxed))
+
 
 template <typename T>
 struct Cplx;

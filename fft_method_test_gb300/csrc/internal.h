@@ -10,9 +10,11 @@
 #include <string>
 #include <vector>
 
+#include "../../include/fftperm.h"
 #include "fft_engine.cuh"
 
 namespace fp {
+
 
 enum Precision { kFP64 = 0, kMixed = 1 };
 
@@ -100,6 +102,8 @@ struct Problem {
     double* d_b = nullptr;
     double* d_x = nullptr;
     double* d_z = nullptr;
+    double* d_r0 = nullptr;    // mixed mode: the refinement segment's FP64 residual
+    double* d_corr = nullptr;  // mixed mode: the segment's start point
     double* d_v[3] = {nullptr, nullptr, nullptr};
     double* d_w[2] = {nullptr, nullptr};
 
@@ -191,15 +195,30 @@ cudaError_t launch_apply(Problem& P, const ApplyArgs& a, int* nparts);
 cudaError_t launch_sum3(Problem& P, const double* v, long long nb, double* out3);
 // Reduce [nparts][4] partials into out4 (deterministic, one block).
 cudaError_t launch_reduce4(Problem& P, int nparts, double* out4);
+// r0_precision: operator precision of r0 = b - A x0 (-1: the problem's own)
 cudaError_t minres_start(Problem& P, const double* b, const double* x0, double tol,
-                         long long maxit);
+                         long long maxit, int r0_precision = -1);
 cudaError_t minres_iteration(Problem& P);
 cudaError_t launch_sub_mean(Problem& P, double* v, const double* sums, double scale);
 // out4[3] = |b - ax|^2
 cudaError_t launch_resnorm(Problem& P, const double* b, const double* ax, double* out4);
+// out = a x + b y over the 3 nb compact entries
+cudaError_t launch_axpby(Problem& P, double* out, double a, const double* x, double b,
+                         const double* y);
 cudaError_t launch_gather_sum(Problem& P, const double* u_dense, double* out4);
 cudaError_t launch_add_const3(Problem& P, double* u_dense, const double* add3);
 cudaError_t launch_background_force(Problem& P, const double cf[3], const double cs[3],
                                     double* f0);
 
+// ---- handles (capi.cu) ----
+// fp_create's body: plans, stream and work buffers; the Green tables only when
+// with_green.  On failure *out still holds the handle with its error message.
+int create_handle(int nx, int ny, int nz, double voxel_size, double mu, int p_radius,
+                  int precision, bool with_green, fp_handle* out);
+
 }  // namespace fp
+
+// The opaque handle of include/fftperm.h.
+struct fp_problem {
+    fp::Problem P;
+};

@@ -196,6 +196,9 @@ __global__ void k_br_sum3(BrGrid g, const double* __restrict__ ux, const double*
 }
 
 }  // namespace
+
+void brinkman_set_error(const std::string& m);
+
 }  // namespace fp
 
 using namespace fp;
@@ -223,6 +226,10 @@ int br_fail(int code, const std::string& m) {
 }
 
 }  // namespace
+
+// Shared with kernels_brinkman_fft.cu: both Brinkman entry families report
+// through fp_brinkman_last_error.
+void fp::brinkman_set_error(const std::string& m) { g_brinkman_error = m; }
 
 extern "C" const char* fp_brinkman_last_error(void) { return g_brinkman_error.c_str(); }
 
@@ -284,20 +291,20 @@ extern "C" int fp_brinkman_solve(int nx, int ny, int nz, const uint32_t* ids, ui
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
-    k_br_momentum<<<blocks, threads, 0, s>>>(g, b.st, b.fluid, fluid_mu, solid_penalty, relaxation,
+    FP_LAUNCHED(); k_br_momentum<<<blocks, threads, 0, s>>>(g, b.st, b.fluid, fluid_mu, solid_penalty, relaxation,
                                              force[0], force[1], force[2], ux, uy, uz, p, sx, sy, sz);
-    k_br_divergence<<<blocks, threads, 0, s>>>(g, b.st, sx, sy, sz, div, b.partials);
-    k_br_jacobi0<<<blocks, threads, 0, s>>>(g, b.st, div, phin);
+    FP_LAUNCHED(); k_br_divergence<<<blocks, threads, 0, s>>>(g, b.st, sx, sy, sz, div, b.partials);
+    FP_LAUNCHED(); k_br_jacobi0<<<blocks, threads, 0, s>>>(g, b.st, div, phin);
     double* a = phin;  // current phi after sweep 1
     double* c = phi;
     for (int k = 1; k < 35; ++k) {
-        k_br_jacobi<<<blocks, threads, 0, s>>>(g, b.st, a, div, c);
+        FP_LAUNCHED(); k_br_jacobi<<<blocks, threads, 0, s>>>(g, b.st, a, div, c);
         double* t = a;
         a = c;
         c = t;
     }
-    k_br_project<<<blocks, threads, 0, s>>>(g, b.st, a, sx, sy, sz, ux, uy, uz, p);
-    k_br_check<<<1, 256, 0, s>>>(b.st, b.partials, blocks, n, tolerance, max_iterations);
+    FP_LAUNCHED(); k_br_project<<<blocks, threads, 0, s>>>(g, b.st, a, sx, sy, sz, ux, uy, uz, p);
+    FP_LAUNCHED(); k_br_check<<<1, 256, 0, s>>>(b.st, b.partials, blocks, n, tolerance, max_iterations);
     cudaError_t e = cudaStreamEndCapture(s, &graph);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
     if (e != cudaSuccess) {
@@ -325,7 +332,7 @@ extern "C" int fp_brinkman_solve(int nx, int ny, int nz, const uint32_t* ids, ui
     }
     // superficial velocity (FluidBrinkman.cpp:233-258)
     if (rc == FP_OK) {
-        k_br_sum3<<<blocks, threads, 0, s>>>(g, ux, uy, uz, b.partials);
+        FP_LAUNCHED(); k_br_sum3<<<blocks, threads, 0, s>>>(g, ux, uy, uz, b.partials);
         std::vector<double> part(4 * (size_t)blocks);
         cudaMemcpyAsync(part.data(), b.partials, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, s);
         cudaStreamSynchronize(s);

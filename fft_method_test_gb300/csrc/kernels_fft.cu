@@ -953,13 +953,13 @@ static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
 #define FP_LAUNCH_TMA(kern, grid, threads, smem, map, args, tt)                                  \
     do {                                                                                          \
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem));     \
-        kern<<<grid, threads, smem, P.stream>>>(*(map), args, tt);                                \
+        FP_LAUNCHED(); kern<<<grid, threads, smem, P.stream>>>(*(map), args, tt);                                \
     } while (0)
 
 #define FP_LAUNCH(kern, grid, threads, smem, args)                                              \
     do {                                                                                          \
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem));     \
-        kern<<<grid, threads, smem, P.stream>>>(args);                                            \
+        FP_LAUNCHED(); kern<<<grid, threads, smem, P.stream>>>(args);                                            \
     } while (0)
 
     if (aa.stage != kStageInverse) {

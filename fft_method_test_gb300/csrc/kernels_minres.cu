@@ -304,13 +304,13 @@ __global__ void k_zmean_from_partials(const double* __restrict__ partials, int n
 
 cudaError_t launch_sum3(Problem& P, const double* v, long long nb, double* out4) {
     const int blocks = vec_blocks(P, 3 * nb);
-    k_sum3<<<blocks, kVecThreads, 0, P.stream>>>(v, nb, P.d_partials);
-    k_reduce4<<<1, 256, 0, P.stream>>>(P.d_partials, blocks, out4);
+    FP_LAUNCHED(); k_sum3<<<blocks, kVecThreads, 0, P.stream>>>(v, nb, P.d_partials);
+    FP_LAUNCHED(); k_reduce4<<<1, 256, 0, P.stream>>>(P.d_partials, blocks, out4);
     return cudaGetLastError();
 }
 
 cudaError_t launch_reduce4(Problem& P, int nparts, double* out4) {
-    k_reduce4<<<1, 512, 0, P.stream>>>(P.d_partials, nparts, out4);
+    FP_LAUNCHED(); k_reduce4<<<1, 512, 0, P.stream>>>(P.d_partials, nparts, out4);
     return cudaGetLastError();
 }
 
@@ -319,7 +319,7 @@ cudaError_t launch_reduce4(Problem& P, int nparts, double* out4) {
 static thread_local long long g_queued = 0;
 
 cudaError_t minres_start(Problem& P, const double* b, const double* x0, double tol,
-                         long long maxit) {
+                         long long maxit, int r0_precision) {
     const long long m = 3 * P.nb;
     MinresScalars init{};
     init.tol = tol;
@@ -333,8 +333,8 @@ cudaError_t minres_start(Problem& P, const double* b, const double* x0, double t
     if (e != cudaSuccess) return e;
     const int blocks = vec_blocks(P, m);
     // |b|
-    k_sum3<<<blocks, kVecThreads, 0, P.stream>>>(b, P.nb, P.d_partials);
-    k_start_norms<<<1, 256, 0, P.stream>>>(P.d_sc, P.d_partials, blocks, 0);
+    FP_LAUNCHED(); k_sum3<<<blocks, kVecThreads, 0, P.stream>>>(b, P.nb, P.d_partials);
+    FP_LAUNCHED(); k_start_norms<<<1, 256, 0, P.stream>>>(P.d_sc, P.d_partials, blocks, 0);
     // x = x0 or 0
     if (x0) {
         cudaMemcpyAsync(P.d_x, x0, sizeof(double) * m, cudaMemcpyDeviceToDevice, P.stream);
@@ -346,19 +346,20 @@ cudaError_t minres_start(Problem& P, const double* b, const double* x0, double t
         a.dst = P.d_z;
         a.src_kind = kSrcCompact;
         a.dst_kind = kDstCompact;
+        a.precision = r0_precision;
         int nparts = 0;
         e = launch_apply(P, a, &nparts);
         if (e != cudaSuccess) return e;
-        k_zmean_from_partials<<<1, 512, 0, P.stream>>>(P.d_partials, nparts, 1.0 / (double)P.nb,
+        FP_LAUNCHED(); k_zmean_from_partials<<<1, 512, 0, P.stream>>>(P.d_partials, nparts, 1.0 / (double)P.nb,
                                                        P.d_red + 4);
-        k_residual0<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, b, P.d_z, P.d_red + 4, m, 1);
+        FP_LAUNCHED(); k_residual0<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, b, P.d_z, P.d_red + 4, m, 1);
     } else {
         cudaMemsetAsync(P.d_x, 0, sizeof(double) * m, P.stream);
-        k_residual0<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, b, P.d_z, nullptr, m, 0);
+        FP_LAUNCHED(); k_residual0<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, b, P.d_z, nullptr, m, 0);
     }
     // beta1 = |r0|
-    k_sum3<<<blocks, kVecThreads, 0, P.stream>>>(P.d_z, P.nb, P.d_partials);
-    k_start_norms<<<1, 256, 0, P.stream>>>(P.d_sc, P.d_partials, blocks, 1);
+    FP_LAUNCHED(); k_sum3<<<blocks, kVecThreads, 0, P.stream>>>(P.d_z, P.nb, P.d_partials);
+    FP_LAUNCHED(); k_start_norms<<<1, 256, 0, P.stream>>>(P.d_sc, P.d_partials, blocks, 1);
     e = cudaMemcpyAsync(P.h_sc, P.d_sc, sizeof(MinresScalars), cudaMemcpyDeviceToHost, P.stream);
     if (e != cudaSuccess) return e;
     e = cudaStreamSynchronize(P.stream);
@@ -395,13 +396,13 @@ cudaError_t minres_start(Problem& P, const double* b, const double* x0, double t
     *P.h_sc = s;
     cudaMemcpyAsync(P.d_sc, P.h_sc, sizeof(MinresScalars), cudaMemcpyHostToDevice, P.stream);
     // v = r0 / beta1 into V[0]; v_old = V[2] = 0; w = 0
-    k_scale_div<<<blocks, kVecThreads, 0, P.stream>>>(P.d_z, P.d_v[0], P.d_sc, m);
+    FP_LAUNCHED(); k_scale_div<<<blocks, kVecThreads, 0, P.stream>>>(P.d_z, P.d_v[0], P.d_sc, m);
     cudaMemsetAsync(P.d_v[2], 0, sizeof(double) * m, P.stream);
     cudaMemsetAsync(P.d_w[0], 0, sizeof(double) * m, P.stream);
     cudaMemsetAsync(P.d_w[1], 0, sizeof(double) * m, P.stream);
     // component sums of v (input mean of the first apply)
-    k_sum3<<<blocks, kVecThreads, 0, P.stream>>>(P.d_v[0], P.nb, P.d_partials);
-    k_reduce4<<<1, 256, 0, P.stream>>>(P.d_partials, blocks, P.d_red + 8);
+    FP_LAUNCHED(); k_sum3<<<blocks, kVecThreads, 0, P.stream>>>(P.d_v[0], P.nb, P.d_partials);
+    FP_LAUNCHED(); k_reduce4<<<1, 256, 0, P.stream>>>(P.d_partials, blocks, P.d_red + 8);
     // copy the three sums into sc->vsum
     cudaMemcpyAsync(&P.d_sc->vsum[0], P.d_red + 8, sizeof(double) * 3, cudaMemcpyDeviceToDevice,
                     P.stream);
@@ -427,13 +428,13 @@ cudaError_t minres_iteration(Problem& P) {
     cudaError_t e = launch_apply(P, a, &nparts);
     if (e != cudaSuccess) return e;
     const double inv_nb = 1.0 / (double)P.nb;
-    k_alpha<<<1, 512, 0, P.stream>>>(P.d_sc, P.d_partials, nparts, inv_nb);
+    FP_LAUNCHED(); k_alpha<<<1, 512, 0, P.stream>>>(P.d_sc, P.d_partials, nparts, inv_nb);
     const int blocks = vec_blocks(P, (P.nb + 1) / 2);
-    k_zupd<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, P.d_z, v, v_old, P.nb, P.d_partials);
-    k_scalar<<<1, 256, 0, P.stream>>>(P.d_sc, P.d_partials, blocks, P.d_hist);
-    k_vwupd<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, P.d_z, v, v_new, w_prev, w, P.d_x, P.nb,
+    FP_LAUNCHED(); k_zupd<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, P.d_z, v, v_old, P.nb, P.d_partials);
+    FP_LAUNCHED(); k_scalar<<<1, 256, 0, P.stream>>>(P.d_sc, P.d_partials, blocks, P.d_hist);
+    FP_LAUNCHED(); k_vwupd<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, P.d_z, v, v_new, w_prev, w, P.d_x, P.nb,
                                                    P.d_partials);
-    k_finish<<<1, 256, 0, P.stream>>>(P.d_sc, P.d_partials, blocks);
+    FP_LAUNCHED(); k_finish<<<1, 256, 0, P.stream>>>(P.d_sc, P.d_partials, blocks);
     return cudaGetLastError();
 }
 
@@ -533,36 +534,50 @@ __global__ void k_resnorm(const double* __restrict__ b, const double* __restrict
 cudaError_t launch_resnorm(Problem& P, const double* b, const double* ax, double* out4) {
     const long long m = 3 * P.nb;
     const int blocks = vec_blocks(P, m);
-    k_resnorm<<<blocks, kVecThreads, 0, P.stream>>>(b, ax, m, P.d_partials);
-    k_reduce4<<<1, 512, 0, P.stream>>>(P.d_partials, blocks, out4);
+    FP_LAUNCHED(); k_resnorm<<<blocks, kVecThreads, 0, P.stream>>>(b, ax, m, P.d_partials);
+    FP_LAUNCHED(); k_reduce4<<<1, 512, 0, P.stream>>>(P.d_partials, blocks, out4);
+    return cudaGetLastError();
+}
+
+static __global__ void k_axpby(double* __restrict__ out, double a, const double* __restrict__ x, double b,
+                        const double* __restrict__ y, long long m) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+         i += (long long)gridDim.x * blockDim.x)
+        out[i] = a * x[i] + b * y[i];
+}
+
+cudaError_t launch_axpby(Problem& P, double* out, double a, const double* x, double b,
+                         const double* y) {
+    const long long m = 3 * P.nb;
+    FP_LAUNCHED(); k_axpby<<<vec_blocks(P, m), kVecThreads, 0, P.stream>>>(out, a, x, b, y, m);
     return cudaGetLastError();
 }
 
 cudaError_t launch_sub_mean(Problem& P, double* v, const double* sums, double scale) {
     const long long m = 3 * P.nb;
-    k_sub_mean<<<vec_blocks(P, m), kVecThreads, 0, P.stream>>>(
+    FP_LAUNCHED(); k_sub_mean<<<vec_blocks(P, m), kVecThreads, 0, P.stream>>>(
         v, m, sums, P.nb > 0 ? 1.0 / (double)P.nb : 0.0, scale);
     return cudaGetLastError();
 }
 
 cudaError_t launch_gather_sum(Problem& P, const double* u_dense, double* out4) {
     const int blocks = vec_blocks(P, P.nb);
-    k_gather_sum<<<blocks, kVecThreads, 0, P.stream>>>(u_dense, P.n, P.d_support, P.nb,
+    FP_LAUNCHED(); k_gather_sum<<<blocks, kVecThreads, 0, P.stream>>>(u_dense, P.n, P.d_support, P.nb,
                                                         P.d_partials);
-    k_reduce4<<<1, 512, 0, P.stream>>>(P.d_partials, blocks, out4);
+    FP_LAUNCHED(); k_reduce4<<<1, 512, 0, P.stream>>>(P.d_partials, blocks, out4);
     return cudaGetLastError();
 }
 
 cudaError_t launch_add_const3(Problem& P, double* u_dense, const double* add3) {
-    k_add_const3<<<vec_blocks(P, 3 * P.n), kVecThreads, 0, P.stream>>>(u_dense, P.n, add3);
+    FP_LAUNCHED(); k_add_const3<<<vec_blocks(P, 3 * P.n), kVecThreads, 0, P.stream>>>(u_dense, P.n, add3);
     return cudaGetLastError();
 }
 
 cudaError_t launch_background_force(Problem& P, const double cf[3], const double cs[3],
                                     double* f0) {
-    k_background_force<<<vec_blocks(P, P.n), kVecThreads, 0, P.stream>>>(
+    FP_LAUNCHED(); k_background_force<<<vec_blocks(P, P.n), kVecThreads, 0, P.stream>>>(
         P.d_mask, P.n, P.d_support, P.nb, cf[0], cf[1], cf[2], cs[0], cs[1], cs[2], f0);
-    k_background_force_support<<<vec_blocks(P, P.nb), kVecThreads, 0, P.stream>>>(
+    FP_LAUNCHED(); k_background_force_support<<<vec_blocks(P, P.nb), kVecThreads, 0, P.stream>>>(
         P.d_support, P.nb, P.n, cs[0], cs[1], cs[2], f0);
     return cudaGetLastError();
 }

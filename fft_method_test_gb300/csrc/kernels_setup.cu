@@ -132,9 +132,9 @@ cudaError_t launch_support(Problem& P) {
     if (e != cudaSuccess) return e;
     e = cudaMallocAsync(&d_nf, sizeof(long long), P.stream);
     if (e != cudaSuccess) return e;
-    k_support_count<<<blocks, threads, 0, P.stream>>>(P.d_mask, P.nx, P.ny, P.nz, P.nrows,
+    FP_LAUNCHED(); k_support_count<<<blocks, threads, 0, P.stream>>>(P.d_mask, P.nx, P.ny, P.nz, P.nrows,
                                                       P.support_mode, P.d_row_cnt, d_fluid);
-    k_scan_rows<<<1, 1024, 0, P.stream>>>(P.d_row_cnt, d_fluid, P.nrows, P.d_row_ptr, d_nf);
+    FP_LAUNCHED(); k_scan_rows<<<1, 1024, 0, P.stream>>>(P.d_row_cnt, d_fluid, P.nrows, P.d_row_ptr, d_nf);
     int nb = 0;
     long long nf = 0;
     cudaMemcpyAsync(&nb, P.d_row_ptr + P.nrows, sizeof(int), cudaMemcpyDeviceToHost, P.stream);
@@ -148,7 +148,7 @@ cudaError_t launch_support(Problem& P) {
     if (P.d_support) cudaFreeAsync(P.d_support, P.stream);
     e = cudaMallocAsync(&P.d_support, sizeof(int) * (size_t)(nb > 0 ? nb : 1), P.stream);
     if (e != cudaSuccess) return e;
-    k_support_write<<<blocks, threads, 0, P.stream>>>(P.d_mask, P.nx, P.ny, P.nz, P.nrows,
+    FP_LAUNCHED(); k_support_write<<<blocks, threads, 0, P.stream>>>(P.d_mask, P.nx, P.ny, P.nz, P.nrows,
                                                       P.support_mode, P.d_row_ptr, P.d_support);
     return cudaGetLastError();
 }
@@ -314,7 +314,7 @@ cudaError_t launch_green(Problem& P, double* g64, float* g32) {
 cudaError_t launch_green_kernel(const GreenArgs& a, cudaStream_t stream) {
     const int threads = 128;
     const long long blocks = (a.nh + threads - 1) / threads;
-    k_green<<<(unsigned)blocks, threads, 0, stream>>>(a);
+    FP_LAUNCHED(); k_green<<<(unsigned)blocks, threads, 0, stream>>>(a);
     return cudaGetLastError();
 }
 

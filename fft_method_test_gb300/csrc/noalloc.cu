@@ -145,8 +145,8 @@ extern "C" int fp_green_apply_noalloc(int nx, int ny, int nz, double voxel_size,
         plans[a]->tw32 = tw32 + a * kNoAllocMaxEdge;
     }
     const int maxe = nx > ny ? (nx > nz ? nx : nz) : (ny > nz ? ny : nz);
-    k_noalloc_twiddles<<<(maxe + 127) / 128, 128, 0, s>>>(nx, ny, nz, tw64, tw32);
-    k_noalloc_tables<<<(maxe + 127) / 128, 128, 0, s>>>(nx, ny, nz, voxel_size, pr, tab);
+    FP_LAUNCHED(); k_noalloc_twiddles<<<(maxe + 127) / 128, 128, 0, s>>>(nx, ny, nz, tw64, tw32);
+    FP_LAUNCHED(); k_noalloc_tables<<<(maxe + 127) / 128, 128, 0, s>>>(nx, ny, nz, voxel_size, pr, tab);
 
     P.nx = nx;
     P.ny = ny;

@@ -70,6 +70,10 @@ const char* fp_last_error(fp_handle h);
 void* fp_stream(fp_handle h);
 /* Wait for all work queued on the handle's stream. */
 int fp_synchronize(fp_handle h);
+/* Number of CUDA kernels this library has launched in the process so far
+ * (every handle, device and stream).  A diagnostic with no counterpart in the
+ * reference: the difference across a region counts the kernels it queued. */
+long long fp_kernel_launch_count(void);
 /* Precision of later applies/solves (FP_PREC_*). */
 int fp_set_precision(fp_handle h, int precision);
 
@@ -178,6 +182,29 @@ int fp_brinkman_permeability(int nx, int ny, int nz, const uint32_t* ids, uint32
                              double tolerance, int max_iterations, double forcing,
                              double voxel_size, double K[9], fp_brinkman_stats stats[3]);
 const char* fp_brinkman_last_error(void);
+
+/* The same Brinkman problem solved to the discrete fixed point of the
+ * reference's equations, (alpha + 6 mu) u - mu sum_nbr u + grad_c p = f and
+ * div_c u = 0 (the state where FluidBrinkman.cpp:313-369 and :402-466 are at
+ * rest), by an FFT-preconditioned projected conjugate gradient, FP64.  The
+ * reference iteration converges like iter^-1.2 toward that point and stalls
+ * far above tolerances such as 1e-8; this entry reaches them.  No reference
+ * counterpart as a function: it replaces solveBrinkman where the caller wants
+ * the converged field.  Arguments as fp_brinkman_solve without relaxation;
+ * tolerance bounds the projected momentum residual |P(f - A u)| / |P f|
+ * (stats->residual).  p receives the pressure with zero mean on the modes
+ * grad_c cannot see.  Needs fluid_mu == 1 (the solid's viscosity): other
+ * values return FP_ERR_UNSUPPORTED. */
+int fp_brinkman_fft_solve(int nx, int ny, int nz, const uint32_t* ids, uint32_t fluid_id,
+                          double fluid_mu, double solid_penalty, double tolerance,
+                          int max_iterations, const double force[3], double* ux, double* uy,
+                          double* uz, double* p, double U[3], fp_brinkman_stats* stats);
+/* computePermeabilityTensor (src/brinkman/FluidBrinkman.cpp:509-553) on
+ * fp_brinkman_fft_solve: one device set-up, three load cases. */
+int fp_brinkman_fft_permeability(int nx, int ny, int nz, const uint32_t* ids, uint32_t fluid_id,
+                                 double fluid_mu, double solid_penalty, double tolerance,
+                                 int max_iterations, double forcing, double voxel_size,
+                                 double K[9], fp_brinkman_stats stats[3]);
 
 #ifdef __cplusplus
 }

@@ -312,9 +312,9 @@ def test_mixed_precision_apply_accuracy(gpu_lib, restatement):
 
 
 def test_mixed_precision_permeability_within_1e6(gpu_lib, restatement):
-    """Mixed precision with reliable updates (true residual every 20
-    iterations): K within 1e-6 of the FP64 oracle's K (tol 1e-10), and the
-    reported residual is the true one."""
+    """Mixed precision (FP32 operator inside FP64 iterative refinement): K
+    within 1e-6 of the FP64 oracle's K (tol 1e-10), and every load case
+    converged on its FP64 residual."""
     mask = G.spheres(32, 4.0, 0.60, seed=1001)
     K_ref, _ = restatement.context(mask).solve_permeability(1e-10, 2000)
     with problem(mask.shape, precision="mixed") as p:
@@ -322,4 +322,21 @@ def test_mixed_precision_permeability_within_1e6(gpu_lib, restatement):
         K, stats = p.solve_permeability(1e-7, 4000)
     assert rel_err(K, K_ref) < 1e-6, rel_err(K, K_ref)
     for s in stats:
-        assert s["converged"] and s["final_rel_residual"] <= 1e-7
+        assert s["converged"] and s["final_rel_residual"] <= 1e-7, stats
+
+
+def test_mixed_precision_minres_reaches_fp64_tolerance(gpu_lib, restatement):
+    """Mixed mode reaches a tolerance far below the FP32 operator's accuracy:
+    the returned iterate's residual, recomputed by the FP64 oracle, is below
+    tol and equals the reported one."""
+    mask = make_geom("sph16")
+    ctx = restatement.context(mask)
+    tol = 1e-10
+    with problem(mask.shape, precision="mixed") as p:
+        p.set_geometry(mask)
+        b = p.build_rhs((1.0, 0.0, 0.0))
+        r = p.minres(b, tol, 4000)
+    assert r.converged, r.final_rel_residual
+    true_rel = np.linalg.norm(b - ctx.operator_apply(r.solution)) / np.linalg.norm(b)
+    assert true_rel <= 1.05 * tol, true_rel
+    assert abs(true_rel - r.final_rel_residual) <= 0.05 * tol
