@@ -401,3 +401,47 @@ def computePermeabilityTensor(ids: np.ndarray, fluid_id: int = 1, fluid_mu: floa
                                       stats)
     _brinkman_check(lib, rc)
     return K.reshape(3, 3), [s.as_dict() for s in stats]
+
+
+def solveBrinkmanFixedPoint(ids: np.ndarray, force, fluid_id: int = 1, fluid_mu: float = 1.0,
+                            solid_penalty: float = 1.0e8, tolerance: float = 1.0e-8,
+                            max_iterations: int = 20000, want_fields: bool = False) -> dict:
+    """The Brinkman problem of solveBrinkman solved to the discrete fixed point
+    of the reference's equations (fp_brinkman_fft_solve: FFT-preconditioned
+    projected conjugate gradient, FP64).  residual = |P(f - A u)| / |P f|."""
+    lib = _capi.load()
+    ids = np.ascontiguousarray(ids, dtype=np.uint32)
+    nz, ny, nx = ids.shape
+    n = ids.size
+    fields = [np.zeros(n) for _ in range(4)] if want_fields else None
+    U = np.zeros(3)
+    st = _capi.BrinkmanStats()
+    ptrs = [f.ctypes.data for f in fields] if want_fields else [None] * 4
+    rc = lib.fp_brinkman_fft_solve(nx, ny, nz, ids.ravel(), int(fluid_id), float(fluid_mu),
+                                   float(solid_penalty), float(tolerance), int(max_iterations),
+                                   np.asarray(force, np.float64), *ptrs, U, C.byref(st))
+    _brinkman_check(lib, rc)
+    out = dict(superficialVelocity=U, **st.as_dict())
+    if want_fields:
+        out.update(ux=fields[0].reshape(ids.shape), uy=fields[1].reshape(ids.shape),
+                   uz=fields[2].reshape(ids.shape), p=fields[3].reshape(ids.shape))
+    return out
+
+
+def computePermeabilityTensorFixedPoint(ids: np.ndarray, fluid_id: int = 1, fluid_mu: float = 1.0,
+                                        solid_penalty: float = 1.0e8, tolerance: float = 1.0e-8,
+                                        max_iterations: int = 20000, forcing: float = 1.0,
+                                        voxel_size: float = 1.0):
+    """computePermeabilityTensor on the fixed-point solver: (K 3x3, [stats] * 3)."""
+    lib = _capi.load()
+    ids = np.ascontiguousarray(ids, dtype=np.uint32)
+    nz, ny, nx = ids.shape
+    K = np.zeros(9)
+    stats = (_capi.BrinkmanStats * 3)()
+    rc = lib.fp_brinkman_fft_permeability(nx, ny, nz, ids.ravel(), int(fluid_id), float(fluid_mu),
+                                          float(solid_penalty), float(tolerance),
+                                          int(max_iterations), float(forcing), float(voxel_size),
+                                          K, stats)
+    _brinkman_check(lib, rc)
+    return K.reshape(3, 3), [s.as_dict() for s in stats]
+

@@ -85,3 +85,83 @@ def test_brinkman_errors(gpu_lib):
     with pytest.raises(FpError) as ei:
         brinkman(ids, (1, 0, 0), solid_penalty=1e4, relaxation=3.5, max_iterations=20000)
     assert "unstable" in str(ei.value)
+
+
+# ---- the fixed point of the same equations (fp_brinkman_fft_solve) ----------
+
+def fixed_point(*a, **k):
+    from fft_method_test_gb300.permeability import solveBrinkmanFixedPoint
+
+    return solveBrinkmanFixedPoint(*a, **k)
+
+
+@pytest.mark.parametrize("shape,seed,force", [((12, 12, 12), 5, (1.0, 0.0, 0.0)),
+                                              ((16, 16, 16), 6, (0.3, -1.0, 0.5)),
+                                              ((10, 12, 8), 7, (0.0, 0.0, 2.0))])
+def test_fixed_point_matches_direct_kkt_solve(gpu_lib, shape, seed, force):
+    """Velocity equal to the direct sparse solve of the reference's discrete
+    equations (oracle/brinkman_kkt.py) within 1e-8 relative; the pressure
+    satisfies the momentum equation with it."""
+    import brinkman_kkt as BK
+
+    rng = np.random.default_rng(seed)
+    mask = (rng.random(shape) >= 0.45).astype(np.uint8)
+    ids = G.to_ids(mask)
+    k = BK.solve(ids, solid_penalty=1e4, force=force)
+    r = fixed_point(ids, force, solid_penalty=1e4, tolerance=1e-12, max_iterations=20000,
+                    want_fields=True)
+    assert r["converged"] and r["residual"] <= 1e-12
+    for c in ("ux", "uy", "uz"):
+        assert rel_err(r[c], k[c]) < 1e-8, c
+    assert rel_err(r["superficialVelocity"], k["U"]) < 1e-9
+    u = np.array([r["ux"], r["uy"], r["uz"]])
+    mom, div = BK.residuals(ids, u, r["p"], solid_penalty=1e4, force=force)
+    assert mom < 1e-7 * max(1.0, np.abs(force).max()) and div < 1e-10
+
+
+def test_fixed_point_is_where_the_gpu_reference_scheme_goes(gpu_lib):
+    """The reference scheme (kernels_brinkman.cu) run longer approaches the
+    fixed point monotonically."""
+    mask = G.spheres(16, 2.5, 0.6, seed=11)
+    ids = G.to_ids(mask)
+    fp_ = fixed_point(ids, (1.0, 0.0, 0.0), solid_penalty=1e4, tolerance=1e-11, want_fields=True)
+    errs = []
+    for its in (200, 2000, 8000):
+        r = brinkman(ids, (1.0, 0.0, 0.0), solid_penalty=1e4, tolerance=1e-30, max_iterations=its,
+                     want_fields=True)
+        errs.append(rel_err(r["ux"], fp_["ux"]))
+    assert errs[0] > errs[1] > errs[2]
+    assert errs[2] < 1e-2
+
+
+def test_fixed_point_c2_128(gpu_lib):
+    """C2: 128^3 spheres r=8 at porosity 0.45, penalty 1e4, tol 1e-8 (the
+    tolerance the reference scheme cannot reach): converged, discretely
+    divergence-free, and K symmetric to the solve tolerance."""
+    from fft_method_test_gb300.permeability import computePermeabilityTensorFixedPoint
+
+    g = np.load(GOLDEN)
+    mask = np.unpackbits(g["c2_mask_bits"])[: 128 ** 3].reshape(128, 128, 128).astype(np.uint8)
+    ids = G.to_ids(mask)
+    r = fixed_point(ids, (1.0, 0.0, 0.0), solid_penalty=1e4, tolerance=1e-8, want_fields=True)
+    assert r["converged"] and r["residual"] <= 1e-8
+    div = sum(0.5 * (np.roll(r[c], -1, ax) - np.roll(r[c], 1, ax))
+              for c, ax in (("ux", 2), ("uy", 1), ("uz", 0)))
+    assert np.abs(div).max() < 1e-10 * np.abs(r["ux"]).max()
+    K, st = computePermeabilityTensorFixedPoint(ids, solid_penalty=1e4, tolerance=1e-8)
+    assert all(s["converged"] for s in st)
+    assert np.abs(K - K.T).max() < 1e-6 * np.abs(K).max()
+    assert abs(K[0, 0] - r["superficialVelocity"][0]) < 1e-7 * abs(K[0, 0])
+
+
+def test_fixed_point_errors(gpu_lib):
+    from fft_method_test_gb300 import _capi
+
+    ids = G.to_ids((np.random.default_rng(1).random((8, 8, 8)) > 0.5).astype(np.uint8))
+    with pytest.raises(_capi.FpError) as e:
+        fixed_point(ids, (1.0, 0.0, 0.0), fluid_mu=1.3)
+    assert e.value.code == _capi.FP_ERR_UNSUPPORTED
+    with pytest.raises(_capi.FpError):
+        fixed_point(np.ones((8, 8, 8), np.uint32), (1.0, 0.0, 0.0))
+    with pytest.raises(ValueError):
+        fixed_point(ids, (1.0, 0.0, 0.0), tolerance=0.0)

@@ -231,3 +231,27 @@ def test_fgeo_roundtrip(tmp_path):
     with open(p, "rb") as f:
         raw = f.read()
     assert raw[:4] == b"FGEO" and raw[4] == 1 and raw[5] == 2 and len(raw) == 32 + 2 * m.size
+
+
+def test_brinkman_fixed_point_oracle_is_where_the_reference_scheme_goes(restatement):
+    """The direct KKT solve (oracle/brinkman_kkt.py) satisfies the discrete
+    equations, and the reference's own iteration, run longer and longer,
+    approaches it (error falls with the iteration count)."""
+    import brinkman_kkt as BK
+
+    mask = G.spheres(8, 1.5, 0.6, seed=5)
+    ids = G.to_ids(mask)
+    k = BK.solve(ids)
+    uk = np.array([k["ux"], k["uy"], k["uz"]])
+    mom, div = BK.residuals(ids, uk, k["p"])
+    assert mom < 1e-10 and div < 1e-9
+    import oracle as orc
+
+    checker = orc.Reference() if orc.reference_available() else restatement
+    errs = []
+    for its in (1000, 5000, 20000):
+        o = checker.brinkman(ids, tolerance=1e-30, max_iterations=its, want_fields=True)
+        u = np.array([o["ux"], o["uy"], o["uz"]]).reshape(uk.shape)
+        errs.append(float(np.abs(u - uk).max()))
+    assert errs[0] > errs[1] > errs[2]
+    assert errs[2] < 2e-4
