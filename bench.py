@@ -60,10 +60,12 @@ def parse():
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--mode", default="solve", choices=["solve", "apply"],
+    ap.add_argument("--mode", default="solve", choices=["solve", "apply", "batch"],
                     help="apply: only run --reps operator applies per precision (for profilers)")
     ap.add_argument("--precision", default="mixed,fp64", help="precisions for --mode apply")
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--batch-count", type=int, default=64, help="microstructures for --mode batch")
+    ap.add_argument("--concurrency", type=int, default=8, help="host threads for --mode batch")
     return ap.parse_args()
 
 
@@ -436,10 +438,68 @@ def run_applies(args):
     print("applies done", flush=True)
 
 
+def batch_workload(count: int = 64):
+    """64 microstructures, seeds 2000..2063: edge uniform from {48, 64, 80,
+    96, 128, 160}, porosity uniform in [0.3, 0.8]; even seeds overlapping
+    spheres with radii uniform in [3, 10], odd seeds Gaussian random fields
+    with correlation length 6."""
+    from fft_method_test_gb300 import geometry as G
+
+    masks = []
+    for i in range(count):
+        seed = 2000 + i
+        rng = np.random.default_rng(seed)
+        edge = int(rng.choice([48, 64, 80, 96, 128, 160]))
+        phi = float(rng.uniform(0.3, 0.8))
+        if seed % 2 == 0:
+            masks.append(G.spheres(edge, 3.0, phi, seed=seed, radius_max=10.0))
+        else:
+            masks.append(G.gaussian_field(edge, 6.0, phi, seed=seed))
+    return masks
+
+
+def run_batch(args):
+    """Batched solve of uneven microstructures: voxel-iterations per second
+    over the whole batch, batched (concurrent, autotuned) and one at a time."""
+    import torch
+
+    from fft_method_test_gb300 import _capi
+    from fft_method_test_gb300.permeability import batch_solve_permeability
+
+    masks = batch_workload(args.batch_count)
+    lib = _capi.load()
+    vox = np.array([m.size for m in masks], dtype=np.float64)
+    out = {}
+    for label, conc in (("batched", args.concurrency), ("sequential", 1)):
+        torch.cuda.synchronize()
+        l0 = lib.fp_kernel_launch_count()
+        t0 = time.perf_counter()
+        K, st, status = batch_solve_permeability(masks, precision="mixed", tol=TOL_MIXED,
+                                                 maxit=MAXIT, concurrency=conc, autotune=True)
+        dt = time.perf_counter() - t0
+        its = np.array([sum(s["iterations"] for s in sp) for sp in st], dtype=np.float64)
+        out[label] = dict(seconds=dt, voxel_iterations_per_s=float((vox * its).sum() / dt),
+                          iterations=int(its.sum()), launches=int(lib.fp_kernel_launch_count() - l0),
+                          all_converged=bool(all(all(s["converged"] for s in sp) for sp in st)),
+                          status_ok=bool(all(c == 0 for c in status)))
+    line = {"metric": "batch_voxel_iterations_per_s", "value": out["batched"]["voxel_iterations_per_s"],
+            "unit": "voxel*iter/s", "higher_is_better": True, "n_gpus": 1, "dtype": "fp32+fp64",
+            "data": "synthetic",
+            "config": {"workload": "batch64_edges48-160_spheres_grf_seeds2000-2063",
+                       "count": len(masks), "concurrency": args.concurrency, "tol": TOL_MIXED,
+                       "precision": "mixed", "voxels": int(vox.sum())},
+            "batched": out["batched"], "sequential": out["sequential"],
+            "speedup_vs_sequential": out["sequential"]["seconds"] / out["batched"]["seconds"]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.mode == "apply":
         run_applies(args)
+        return
+    if args.mode == "batch":
+        run_batch(args)
         return
     world, rank, local = dist_setup(args)
     if args.impl == "reference":

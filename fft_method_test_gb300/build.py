@@ -23,6 +23,11 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 NO_FMA = {"kernels_brinkman.cu"}
 
 
+# rough relative compile cost per source, to order the parallel jobs
+_COST = {"fft_ztma32.cu": 10, "fft_z32.cu": 9, "fft_y32.cu": 5, "fft_ztma64.cu": 4,
+         "fft_x32.cu": 3, "fft_z64.cu": 3}
+
+
 def _nvcc() -> str:
     for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
         if cand and os.path.exists(cand):
@@ -66,7 +71,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return cmd
 
     if jobs:
-        with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
+        # the FP32 z passes take minutes (fully unrolled radix-16 code): start
+        # them first so that they overlap everything else
+        jobs.sort(key=lambda c: -_COST.get(os.path.basename(c[-3]), 1))
+        workers = min(len(jobs), max(2, os.cpu_count() or 2), 16)
+        with cf.ThreadPoolExecutor(max_workers=workers) as ex:
             list(ex.map(run, jobs))
     if force or jobs or _stale(LIB, objs):
         run([nvcc, *ARCH, "-shared", "-o", LIB, *objs])

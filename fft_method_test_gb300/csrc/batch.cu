@@ -1,0 +1,266 @@
+// batch.cu -- many independent microstructures solved together, and the FFT
+// tile autotuner.
+//
+// Batching.  Each microstructure is a complete permeability solve (three load
+// cases) with no data shared with the others, so the batch needs no
+// collective: it is a work queue.  `concurrency` host threads each own one
+// handle (its own stream) at a time and run fp_solve_permeability on it;
+// their kernels overlap on the GPU, so the small grids of a batch (48^3 to
+// 160^3 use a few hundred CTAs per pass) fill the 152 SMs together.  Inside a
+// solve the MINRES iterations are replayed as CUDA graphs of 20 (one graph
+// launch per chunk, not nine kernel launches per iteration).  Problems are
+// taken largest first, which keeps the tail of the batch short.
+//
+// Autotuner.  The y and z passes take `tile` kx columns per CTA and have a
+// TMA-fed and a register-fed variant.  fp_autotune times the operator apply
+// of a handle for each candidate and keeps the fastest; results are cached per
+// (grid, precision) for the process.  The batch tunes every distinct grid
+// once before the workers start, so that the timings see an idle GPU.
+// Tiling changes the schedule and the grouping of the x pass's partial sums;
+// each line's transform is the same arithmetic.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <tuple>
+#include <vector>
+
+#include "../../include/fftperm.h"
+#include "internal.h"
+
+namespace fp {
+namespace {
+
+struct TuneKey {
+    int nx, ny, nz, precision;
+    bool operator<(const TuneKey& o) const {
+        return std::tie(nx, ny, nz, precision) < std::tie(o.nx, o.ny, o.nz, o.precision);
+    }
+};
+
+struct TuneResult {
+    int tile = 0;
+    bool tma_off = false;
+    double ms = 0.0;
+};
+
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneResult> g_tune_cache;
+
+thread_local std::string g_batch_error;
+
+void apply_tiling(Problem& P, int tile, bool tma_off) {
+    if (P.tile_yz == tile && P.tma_off == tma_off) return;
+    release_graphs(P);
+    P.tile_yz = tile;
+    P.tma_off = tma_off;
+    for (auto& c : P.tma_y) c.valid = false;
+    for (auto& c : P.tma_z) c.valid = false;
+}
+
+// Mean time of `reps` operator applies (compact source when a geometry is
+// set, dense otherwise) on the handle's stream, after one warm-up apply.
+int time_apply(Problem& P, int reps, double* ms) {
+    ApplyArgs a;
+    if (P.has_geometry && P.nb > 0) {
+        cudaMemsetAsync(P.d_x, 0, sizeof(double) * 3 * (size_t)P.nb, P.stream);
+        a.src = P.d_x;
+        a.dst = P.d_cout;
+        a.src_kind = kSrcCompact;
+        a.dst_kind = kDstCompact;
+    } else {
+        DeviceMemGuard mem_guard;
+        if (!P.d_dense_in && cudaMalloc(&P.d_dense_in, sizeof(double) * 3 * (size_t)P.n) != cudaSuccess)
+            return FP_ERR_NOMEM;
+        if (!P.d_dense_out &&
+            cudaMalloc(&P.d_dense_out, sizeof(double) * 3 * (size_t)P.n) != cudaSuccess)
+            return FP_ERR_NOMEM;
+        cudaMemsetAsync(P.d_dense_in, 0, sizeof(double) * 3 * (size_t)P.n, P.stream);
+        a.src = P.d_dense_in;
+        a.dst = P.d_dense_out;
+        a.src_kind = kSrcDense;
+        a.dst_kind = kDstDense;
+    }
+    int np = 0;
+    if (launch_apply(P, a, &np) != cudaSuccess) return FP_ERR_CUDA;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, P.stream);
+    cudaError_t err = cudaSuccess;
+    for (int i = 0; i < reps && err == cudaSuccess; ++i) err = launch_apply(P, a, &np);
+    cudaEventRecord(e1, P.stream);
+    cudaEventSynchronize(e1);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (err != cudaSuccess) return FP_ERR_CUDA;
+    int herr = 0;
+    cudaMemcpy(&herr, P.d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (herr) return FP_ERR_CUDA;
+    *ms = (double)t / reps;
+    return FP_OK;
+}
+
+int tune(Problem& P, TuneResult* out) {
+    const TuneKey key{P.nx, P.ny, P.nz, P.precision};
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            *out = it->second;
+            apply_tiling(P, out->tile, out->tma_off);
+            return FP_OK;
+        }
+    }
+    const int tile0 = P.tile_yz;
+    const bool tma0 = P.tma_off;
+    TuneResult best;
+    best.ms = 1e30;
+    const int tiles[] = {4, 8, 16, 32};
+    for (int off = 0; off < 2; ++off) {
+        for (int t : tiles) {
+            apply_tiling(P, t, off != 0);
+            double ms = 0.0;
+            const int rc = time_apply(P, 3, &ms);
+            if (rc != FP_OK) {
+                apply_tiling(P, tile0, tma0);
+                return rc;
+            }
+            if (ms < best.ms) {
+                best.ms = ms;
+                best.tile = t;
+                best.tma_off = off != 0;
+            }
+        }
+    }
+    apply_tiling(P, best.tile, best.tma_off);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tune_cache[key] = best;
+    }
+    *out = best;
+    return FP_OK;
+}
+
+struct Job {
+    int index;
+    long long voxels;
+};
+
+}  // namespace
+}  // namespace fp
+
+extern "C" int fp_autotune(fp_handle h, int* tile, int* tma_off, double* apply_ms) {
+    using namespace fp;
+    if (!h) return FP_ERR_INVALID;
+    TuneResult r;
+    const int rc = tune(h->P, &r);
+    if (rc != FP_OK) {
+        h->P.err = "autotune: an operator apply failed";
+        return rc;
+    }
+    if (tile) *tile = r.tile;
+    if (tma_off) *tma_off = r.tma_off ? 1 : 0;
+    if (apply_ms) *apply_ms = r.ms;
+    return FP_OK;
+}
+
+extern "C" const char* fp_batch_last_error(void) { return fp::g_batch_error.c_str(); }
+
+extern "C" int fp_batch_solve_permeability(int count, const int* dims, const uint8_t* const* masks,
+                                           const double* voxel_sizes, double mu, int p_radius,
+                                           int precision, int support_mode, double tol,
+                                           int64_t maxit, int concurrency, int autotune, double* K,
+                                           fp_solver_stats* stats, int* status) {
+    using namespace fp;
+    g_batch_error.clear();
+    if (count < 0 || (count > 0 && (!dims || !masks || !K)) || concurrency < 1) {
+        g_batch_error = "batch: invalid arguments";
+        return FP_ERR_INVALID;
+    }
+    for (int i = 0; i < count; ++i)
+        if (dims[3 * i] <= 0 || dims[3 * i + 1] <= 0 || dims[3 * i + 2] <= 0 || !masks[i]) {
+            g_batch_error = "batch: problem " + std::to_string(i) + " has invalid dimensions or mask";
+            return FP_ERR_INVALID;
+        }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        g_batch_error = "batch: no CUDA device";
+        return FP_ERR_CUDA;
+    }
+    auto make = [&](int i, fp_handle* h) -> int {
+        const double vs = voxel_sizes ? voxel_sizes[i] : 1.0;
+        int rc = fp_create(dims[3 * i], dims[3 * i + 1], dims[3 * i + 2], vs, mu, p_radius, precision, h);
+        if (rc == FP_OK) rc = fp_set_geometry(*h, masks[i], support_mode, nullptr);
+        return rc;
+    };
+    // 1) tune each distinct grid once, on an otherwise idle GPU
+    if (autotune) {
+        std::map<TuneKey, int> first;
+        for (int i = 0; i < count; ++i) first.emplace(TuneKey{dims[3 * i], dims[3 * i + 1], dims[3 * i + 2], precision}, i);
+        for (auto& kv : first) {
+            fp_handle h = nullptr;
+            int rc = make(kv.second, &h);
+            if (rc == FP_OK) {
+                TuneResult r;
+                rc = tune(h->P, &r);
+            }
+            if (rc != FP_OK) {
+                g_batch_error = "batch: autotune of problem " + std::to_string(kv.second) + ": " +
+                                (h ? h->P.err : std::string("create failed"));
+                fp_destroy(h);
+                return rc;
+            }
+            fp_destroy(h);
+        }
+    }
+    // 2) largest first
+    std::vector<Job> jobs((size_t)count);
+    for (int i = 0; i < count; ++i)
+        jobs[(size_t)i] = Job{i, (long long)dims[3 * i] * dims[3 * i + 1] * dims[3 * i + 2]};
+    std::stable_sort(jobs.begin(), jobs.end(), [](const Job& a, const Job& b) { return a.voxels > b.voxels; });
+    std::atomic<int> next{0};
+    std::vector<int> rcs((size_t)count, FP_OK);
+    std::vector<std::string> errs((size_t)count);
+    auto worker = [&]() {
+        cudaSetDevice(dev);
+        for (;;) {
+            const int j = next.fetch_add(1);
+            if (j >= count) return;
+            const int i = jobs[(size_t)j].index;
+            fp_handle h = nullptr;
+            int rc = make(i, &h);
+            if (rc == FP_OK && autotune) {
+                TuneResult r;
+                rc = tune(h->P, &r);  // a cache hit: sets the tuned tiling
+            }
+            fp_solver_stats st[3] = {};
+            if (rc == FP_OK) rc = fp_solve_permeability(h, tol, maxit, K + 9 * (size_t)i, st);
+            if (rc == FP_OK && stats)
+                for (int c = 0; c < 3; ++c) stats[3 * (size_t)i + c] = st[c];
+            if (rc != FP_OK) errs[(size_t)i] = h ? h->P.err : std::string("create failed");
+            rcs[(size_t)i] = rc;
+            fp_destroy(h);
+        }
+    };
+    const int nthreads = std::min(concurrency, std::max(count, 1));
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthreads; ++t) pool.emplace_back(worker);
+    for (auto& t : pool) t.join();
+    int first_rc = FP_OK;
+    for (int i = 0; i < count; ++i) {
+        if (status) status[i] = rcs[(size_t)i];
+        if (rcs[(size_t)i] != FP_OK && first_rc == FP_OK) {
+            first_rc = rcs[(size_t)i];
+            g_batch_error = "batch: problem " + std::to_string(i) + ": " + errs[(size_t)i];
+        }
+    }
+    return first_rc;
+}

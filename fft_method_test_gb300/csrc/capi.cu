@@ -12,6 +12,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <shared_mutex>
 #include <string>
 #include <vector>
 
@@ -19,6 +20,21 @@
 #include "internal.h"
 
 std::atomic<long long> fp::g_kernel_launches{0};
+thread_local long long fp::g_thread_launches = 0;
+
+namespace {
+std::shared_mutex g_device_mem_mu;
+thread_local int g_device_mem_depth = 0;
+}  // namespace
+
+fp::DeviceMemGuard::DeviceMemGuard() {
+    if (g_device_mem_depth++ == 0) g_device_mem_mu.lock();
+}
+fp::DeviceMemGuard::~DeviceMemGuard() {
+    if (--g_device_mem_depth == 0) g_device_mem_mu.unlock();
+}
+fp::CaptureGuard::CaptureGuard() { g_device_mem_mu.lock_shared(); }
+fp::CaptureGuard::~CaptureGuard() { g_device_mem_mu.unlock_shared(); }
 
 namespace {
 
@@ -46,6 +62,8 @@ cudaError_t dalloc(T** p, size_t count) {
 }
 
 void free_geometry(Problem& P) {
+    fp::DeviceMemGuard mem_guard_;
+    fp::release_graphs(P);
     cudaFree(P.d_support);
     cudaFree(P.d_cin);
     cudaFree(P.d_cout);
@@ -80,12 +98,14 @@ int check_device_error(Problem& P) {
 }
 
 int alloc_dense(Problem& P) {
+    fp::DeviceMemGuard mem_guard_;
     if (!P.d_dense_in) FP_CUDA(dalloc(&P.d_dense_in, 3 * (size_t)P.n), "cudaMalloc dense");
     if (!P.d_dense_out) FP_CUDA(dalloc(&P.d_dense_out, 3 * (size_t)P.n), "cudaMalloc dense");
     return FP_OK;
 }
 
 int ensure_green32(Problem& P) {
+    fp::DeviceMemGuard mem_guard_;
     if (P.d_green32) return FP_OK;
     FP_CUDA(dalloc(&P.d_green32, 6 * (size_t)P.nh), "cudaMalloc green32");
     FP_CUDA(fp::launch_green(P, nullptr, P.d_green32), "green precompute");
@@ -93,6 +113,7 @@ int ensure_green32(Problem& P) {
 }
 
 int ensure_green64(Problem& P) {
+    fp::DeviceMemGuard mem_guard_;
     if (P.d_green64) return FP_OK;
     FP_CUDA(dalloc(&P.d_green64, 6 * (size_t)P.nh), "cudaMalloc green64");
     FP_CUDA(fp::launch_green(P, P.d_green64, nullptr), "green precompute");
@@ -102,6 +123,7 @@ int ensure_green64(Problem& P) {
 // Mixed mode needs both tables: FP32 for the Krylov applies, FP64 for the
 // residuals that start and end each refinement segment.  One launch fills both.
 int ensure_green_both(Problem& P) {
+    fp::DeviceMemGuard mem_guard_;
     if (P.d_green32 && P.d_green64) return FP_OK;
     if (P.d_green32) return ensure_green64(P);
     if (P.d_green64) return ensure_green32(P);
@@ -202,6 +224,8 @@ int device_minres(Problem& P, const double* d_b, const double* d_x0, double tol,
                   double* hist_host, fp_solver_stats* st) {
     if (!(tol > 0.0)) return fail(P, FP_ERR_INVALID, "MinresSolver tolerance must be positive");
     if (maxit + 1 > P.hist_cap) {
+        fp::DeviceMemGuard mem_guard_;
+        fp::release_graphs(P);  // the graphs write the history through the old pointer
         cudaFree(P.d_hist);
         P.d_hist = nullptr;
         FP_CUDA(dalloc(&P.d_hist, (size_t)maxit + 1), "cudaMalloc hist");
@@ -236,7 +260,7 @@ int device_minres(Problem& P, const double* d_b, const double* d_x0, double tol,
     const int max_restarts = 20;
     for (;;) {
         if (!P.h_sc->done) {
-            for (int i = 0; i < chunk; ++i) FP_CUDA(fp::minres_iteration(P), "minres_iteration");
+            FP_CUDA(fp::minres_iterations(P, chunk), "minres_iteration");
             int rc = read_scalars(P);
             if (rc) return rc;
         }
@@ -354,6 +378,7 @@ int fp_create(int nx, int ny, int nz, double voxel_size, double mu, int p_radius
 
 int fp::create_handle(int nx, int ny, int nz, double voxel_size, double mu, int p_radius,
                       int precision, bool with_green, fp_handle* out) {
+    fp::DeviceMemGuard mem_guard_;
     if (!out) return FP_ERR_INVALID;
     *out = nullptr;
     fp_problem* h = new (std::nothrow) fp_problem();
@@ -385,6 +410,7 @@ int fp::create_handle(int nx, int ny, int nz, double voxel_size, double mu, int 
     FP_CUDA(cudaStreamCreateWithFlags(&P.stream, cudaStreamNonBlocking), "stream");
     if (const char* t = std::getenv("FFTPERM_TILE_YZ")) P.tile_yz = std::atoi(t);
     if (const char* t = std::getenv("FFTPERM_NO_TMA")) P.tma_off = std::atoi(t) != 0;
+    if (const char* t = std::getenv("FFTPERM_NO_GRAPHS")) P.use_graphs = std::atoi(t) == 0;
     std::string err;
     if (!fp::make_axis_plan(nx, P.px, err) || !fp::make_axis_plan(ny, P.py, err) ||
         !fp::make_axis_plan(nz, P.pz, err))
@@ -409,6 +435,7 @@ int fp::create_handle(int nx, int ny, int nz, double voxel_size, double mu, int 
 extern "C" {
 
 int fp_destroy(fp_handle h) {
+    fp::DeviceMemGuard mem_guard_;
     if (!h) return FP_OK;
     Problem& P = h->P;
     if (P.stream) cudaStreamSynchronize(P.stream);
@@ -457,11 +484,13 @@ int fp_set_precision(fp_handle h, int precision) {
         return fail(P, FP_ERR_INVALID, "unknown precision mode");
     int rc = (precision == FP_PREC_MIXED) ? ensure_green_both(P) : ensure_green64(P);
     if (rc) return rc;
+    if (precision != P.precision) fp::release_graphs(P);
     P.precision = precision;
     return FP_OK;
 }
 
 int fp_set_geometry(fp_handle h, const uint8_t* fluid_mask, int support_mode, int64_t* nb_out) {
+    fp::DeviceMemGuard mem_guard_;
     if (!h) return FP_ERR_INVALID;
     Problem& P = h->P;
     if (!fluid_mask) return fail(P, FP_ERR_INVALID, "BinaryMedium mask must not be null");

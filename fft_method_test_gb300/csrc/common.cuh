@@ -11,7 +11,29 @@ namespace fp {
 // Process-wide count of this library's kernel launches (all devices and
 // streams), read by fp_kernel_launch_count.  Every launch site bumps it.
 extern std::atomic<long long> g_kernel_launches;
-#define FP_LAUNCHED() (::fp::g_kernel_launches.fetch_add(1, std::memory_order_relaxed))
+// The calling thread's own launches (a stream capture subtracts what it
+// recorded: other threads keep launching meanwhile).
+extern thread_local long long g_thread_launches;
+#define FP_LAUNCHED() \
+    (++::fp::g_thread_launches, ::fp::g_kernel_launches.fetch_add(1, std::memory_order_relaxed))
+
+// ---- device memory vs graph capture (capi.cu) ----
+// cudaMalloc / cudaFree may synchronise the whole device, which invalidates a
+// stream capture running in another host thread.  Every allocation or free
+// site holds DeviceMemGuard (exclusive, re-entrant within a thread); every
+// capture holds CaptureGuard (shared: captures in different threads overlap).
+struct DeviceMemGuard {
+    DeviceMemGuard();
+    ~DeviceMemGuard();
+    DeviceMemGuard(const DeviceMemGuard&) = delete;
+    DeviceMemGuard& operator=(const DeviceMemGuard&) = delete;
+};
+struct CaptureGuard {
+    CaptureGuard();
+    ~CaptureGuard();
+    CaptureGuard(const CaptureGuard&) = delete;
+    CaptureGuard& operator=(const CaptureGuard&) = delete;
+};
 
 
 template <typename T>

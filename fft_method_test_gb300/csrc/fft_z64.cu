@@ -1,0 +1,9 @@
+// fft_z64.cu -- the register-fed z pass (P3; also the forward-only and
+// inverse-only z transforms) in FP64, one translation unit of the apply
+// (fft_passes.cuh).
+#define FP_DEFINE_Z_RUNNERS
+#include "fft_passes.cuh"
+
+namespace fp {
+template cudaError_t run_zgreen<double>(int, const ZArgs&, dim3, int, size_t, cudaStream_t);
+}  // namespace fp

@@ -58,6 +58,15 @@ struct TmaCache {
     CUtensorMap map;
 };
 
+// One instantiated CUDA graph of `count` MINRES iterations starting at buffer
+// rotation phase `phase` (iteration index mod 6).
+struct MinresGraph {
+    cudaGraphExec_t exec = nullptr;
+    int phase = 0;
+    int count = 0;
+    long long kernels = 0;  // kernel nodes, for the launch counter
+};
+
 struct Problem {
     int nx = 0, ny = 0, nz = 0;
     long long n = 0;      // voxels
@@ -117,6 +126,12 @@ struct Problem {
 
     // TMA-fed y and z passes: [precision 0 = FP64, 1 = FP32]
     TmaCache tma_y[2], tma_z[2];
+    // MINRES iteration chunks replayed as CUDA graphs (FFTPERM_NO_GRAPHS=1: off).
+    // Captured pointers and kernels depend on the geometry, the precision and
+    // the tiling: every change of those releases the graphs.
+    bool use_graphs = true;
+    MinresGraph graphs[6];
+    long long queued = 0;  // iterations queued since minres_start (buffer rotation)
     bool tma_off = false;      // FFTPERM_NO_TMA=1 selects the register-fed passes
     int* d_err = nullptr;      // device error flag (a bounded wait gave up)
 
@@ -199,6 +214,8 @@ cudaError_t launch_reduce4(Problem& P, int nparts, double* out4);
 cudaError_t minres_start(Problem& P, const double* b, const double* x0, double tol,
                          long long maxit, int r0_precision = -1);
 cudaError_t minres_iteration(Problem& P);
+cudaError_t minres_iterations(Problem& P, int count);
+void release_graphs(Problem& P);
 cudaError_t launch_sub_mean(Problem& P, double* v, const double* sums, double scale);
 // out4[3] = |b - ax|^2
 cudaError_t launch_resnorm(Problem& P, const double* b, const double* ax, double* out4);

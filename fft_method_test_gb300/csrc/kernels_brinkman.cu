@@ -19,6 +19,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <optional>
 #include <string>
 #include <vector>
 
@@ -211,6 +212,7 @@ struct BrBuffers {
     double* partials = nullptr;
     BrState* st = nullptr;
     ~BrBuffers() {
+        DeviceMemGuard mem_guard;
         cudaFree(f);
         cudaFree(fluid);
         cudaFree(partials);
@@ -255,11 +257,14 @@ extern "C" int fp_brinkman_solve(int nx, int ny, int nz, const uint32_t* ids, ui
         return br_fail(FP_ERR_STATE, "No fluid material ids found. Set phase=fluid or fluid_material_id.");
     if (nfl == n) return br_fail(FP_ERR_STATE, "No solid material ids found for Brinkman solve.");
     BrBuffers b;
-    if (cudaMalloc(&b.f, sizeof(double) * 10 * (size_t)n) != cudaSuccess ||
-        cudaMalloc(&b.fluid, (size_t)n) != cudaSuccess ||
-        cudaMalloc(&b.partials, sizeof(double) * 4 * 4096) != cudaSuccess ||
-        cudaMalloc(&b.st, sizeof(BrState)) != cudaSuccess)
-        return br_fail(FP_ERR_NOMEM, "solveBrinkman: device allocation failed");
+    {
+        DeviceMemGuard mem_guard;
+        if (cudaMalloc(&b.f, sizeof(double) * 10 * (size_t)n) != cudaSuccess ||
+            cudaMalloc(&b.fluid, (size_t)n) != cudaSuccess ||
+            cudaMalloc(&b.partials, sizeof(double) * 4 * 4096) != cudaSuccess ||
+            cudaMalloc(&b.st, sizeof(BrState)) != cudaSuccess)
+            return br_fail(FP_ERR_NOMEM, "solveBrinkman: device allocation failed");
+    }
     double* ux = b.f;
     double* uy = ux + n;
     double* uz = uy + n;
@@ -290,6 +295,9 @@ extern "C" int fp_brinkman_solve(int nx, int ny, int nz, const uint32_t* ids, ui
     // one outer iteration, captured once and replayed
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    const long long l0 = g_thread_launches;
+    std::optional<CaptureGuard> capture_guard;
+    capture_guard.emplace();
     cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     FP_LAUNCHED(); k_br_momentum<<<blocks, threads, 0, s>>>(g, b.st, b.fluid, fluid_mu, solid_penalty, relaxation,
                                              force[0], force[1], force[2], ux, uy, uz, p, sx, sy, sz);
@@ -307,6 +315,10 @@ extern "C" int fp_brinkman_solve(int nx, int ny, int nz, const uint32_t* ids, ui
     FP_LAUNCHED(); k_br_check<<<1, 256, 0, s>>>(b.st, b.partials, blocks, n, tolerance, max_iterations);
     cudaError_t e = cudaStreamEndCapture(s, &graph);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    capture_guard.reset();
+    // the capture ran nothing: count the graph's kernels at each replay
+    const long long graph_kernels = g_thread_launches - l0;
+    g_kernel_launches.fetch_sub(graph_kernels, std::memory_order_relaxed);
     if (e != cudaSuccess) {
         cudaStreamDestroy(s);
         return br_fail(FP_ERR_CUDA, std::string("solveBrinkman graph: ") + cudaGetErrorString(e));
@@ -323,7 +335,10 @@ extern "C" int fp_brinkman_solve(int nx, int ny, int nz, const uint32_t* ids, ui
             break;
         }
         if (hs->done) break;
-        for (int i = 0; i < chunk; ++i) cudaGraphLaunch(exec, s);
+        for (int i = 0; i < chunk; ++i) {
+            cudaGraphLaunch(exec, s);
+            g_kernel_launches.fetch_add(graph_kernels, std::memory_order_relaxed);
+        }
     }
     BrState fin = *hs;
     if (rc == FP_OK && fin.nonfinite) {

@@ -353,6 +353,7 @@ struct BfSolver {
     BfScalars* hsc = nullptr;
     int blocks = 0;
     ~BfSolver() {
+        DeviceMemGuard mem_guard;
         cudaFree(x);
         cudaFree(p);
         cudaFree(w);
@@ -382,6 +383,7 @@ int bf_init(BfSolver& S, int nx, int ny, int nz, const uint8_t* fl_host) {
     if (rc != FP_OK) return bf_fail(rc, S.h ? S.h->P.err : std::string("handle creation failed"));
     Problem& P = S.h->P;
     const size_t m = 3 * (size_t)P.n;
+    DeviceMemGuard mem_guard;
     BF_CUDA(cudaMalloc(&S.x, sizeof(double) * m), "cudaMalloc");
     BF_CUDA(cudaMalloc(&S.p, sizeof(double) * m), "cudaMalloc");
     BF_CUDA(cudaMalloc(&S.w, sizeof(double) * m), "cudaMalloc");

@@ -184,6 +184,11 @@ __global__ void k_vwupd(const MinresScalars* sc, const double* __restrict__ z, c
     const double step = sc->step;
     const bool vb = beta_new > kBreakdownEps;
     const bool rb = rho > kBreakdownEps;
+    // one division per CTA: GB300's FP64 pipe is narrow, and per-element
+    // divisions made this kernel FP64-bound (x / d becomes x * (1 / d), a
+    // difference of at most one rounding)
+    const double inv_beta = vb ? 1.0 / beta_new : 0.0;
+    const double inv_rho = rb ? 1.0 / rho : 0.0;
     double acc[4] = {0, 0, 0, 0};
     const long long npair = nb >> 1;
     const double2* z2 = reinterpret_cast<const double2*>(z);
@@ -198,10 +203,10 @@ __global__ void k_vwupd(const MinresScalars* sc, const double* __restrict__ z, c
         for (int h = 0; h < 3; ++h) {
             const long long q = 3 * k + h;
             const double2 zz = z2[q], vo = v2[q], wp = wp2[q], ww = w2[q], xx = x2[q];
-            const double vn0 = vb ? zz.x / beta_new : 0.0;
-            const double vn1 = vb ? zz.y / beta_new : 0.0;
-            const double wn0 = rb ? (vo.x - eps * wp.x - delta * ww.x) / rho : 0.0;
-            const double wn1 = rb ? (vo.y - eps * wp.y - delta * ww.y) / rho : 0.0;
+            const double vn0 = zz.x * inv_beta;
+            const double vn1 = zz.y * inv_beta;
+            const double wn0 = (vo.x - eps * wp.x - delta * ww.x) * inv_rho;
+            const double wn1 = (vo.y - eps * wp.y - delta * ww.y) * inv_rho;
             vn2[q] = make_double2(vn0, vn1);
             wp2[q] = make_double2(wn0, wn1);
             x2[q] = make_double2(xx.x + step * wn0, xx.y + step * wn1);
@@ -213,9 +218,9 @@ __global__ void k_vwupd(const MinresScalars* sc, const double* __restrict__ z, c
         for (int c = 0; c < 3; ++c) {
             const long long i = 3 * (nb - 1) + c;
             const double vo = v[i];
-            const double vn = vb ? z[i] / beta_new : 0.0;
+            const double vn = z[i] * inv_beta;
             v_new[i] = vn;
-            const double wn = rb ? (vo - eps * w_prev_to_next[i] - delta * w[i]) / rho : 0.0;
+            const double wn = (vo - eps * w_prev_to_next[i] - delta * w[i]) * inv_rho;
             w_prev_to_next[i] = wn;
             x[i] += step * wn;
             acc[c] += vn;
@@ -314,9 +319,6 @@ cudaError_t launch_reduce4(Problem& P, int nparts, double* out4) {
     return cudaGetLastError();
 }
 
-// Host-side iteration counter of the queued iterations (selects the rotating
-// Lanczos/w buffers); reset by minres_start.
-static thread_local long long g_queued = 0;
 
 cudaError_t minres_start(Problem& P, const double* b, const double* x0, double tol,
                          long long maxit, int r0_precision) {
@@ -328,7 +330,7 @@ cudaError_t minres_start(Problem& P, const double* b, const double* x0, double t
     init.sn_old = 0.0;
     init.cs = -1.0;
     init.sn = 0.0;
-    g_queued = 0;
+    P.queued = 0;
     cudaError_t e = cudaMemcpyAsync(P.d_sc, &init, sizeof(init), cudaMemcpyHostToDevice, P.stream);
     if (e != cudaSuccess) return e;
     const int blocks = vec_blocks(P, m);
@@ -409,8 +411,75 @@ cudaError_t minres_start(Problem& P, const double* b, const double* x0, double t
     return cudaGetLastError();
 }
 
+// Queue `count` iterations, replaying a CUDA graph of them when graphs are on.
+// The buffers rotate with period 6 (three Lanczos vectors, two w vectors), so
+// one graph per (start phase, count) serves every chunk.  The kernel launch
+// counter counts the graph's kernels at each replay.
+cudaError_t minres_iterations(Problem& P, int count) {
+    if (!P.use_graphs || count <= 0) {
+        for (int i = 0; i < count; ++i) {
+            cudaError_t e = minres_iteration(P);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+    const int phase = (int)(P.queued % 6);
+    MinresGraph* slot = nullptr;
+    for (auto& g : P.graphs)
+        if (g.exec && g.phase == phase && g.count == count) slot = &g;
+    if (!slot) {
+        for (auto& g : P.graphs)
+            if (!g.exec) {
+                slot = &g;
+                break;
+            }
+        if (!slot) {
+            release_graphs(P);
+            slot = &P.graphs[0];
+        }
+        const long long q0 = P.queued;
+        CaptureGuard capture_guard;
+        const long long l0 = g_thread_launches;
+        cudaError_t e = cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        cudaError_t le = cudaSuccess;
+        for (int i = 0; i < count && le == cudaSuccess; ++i) le = minres_iteration(P);
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamEndCapture(P.stream, &graph);
+        const long long nk = g_thread_launches - l0;
+        g_kernel_launches.fetch_sub(nk, std::memory_order_relaxed);  // nothing ran yet
+        P.queued = q0;
+        if (le != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return le;
+        }
+        if (e != cudaSuccess) return e;
+        e = cudaGraphInstantiate(&slot->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            slot->exec = nullptr;
+            return e;
+        }
+        slot->phase = phase;
+        slot->count = count;
+        slot->kernels = nk;
+    }
+    cudaError_t e = cudaGraphLaunch(slot->exec, P.stream);
+    if (e != cudaSuccess) return e;
+    g_kernel_launches.fetch_add(slot->kernels, std::memory_order_relaxed);
+    P.queued += count;
+    return cudaSuccess;
+}
+
+void release_graphs(Problem& P) {
+    for (auto& g : P.graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = MinresGraph{};
+    }
+}
+
 cudaError_t minres_iteration(Problem& P) {
-    const long long k = g_queued++;
+    const long long k = P.queued++;
     double* v = P.d_v[k % 3];
     double* v_old = P.d_v[(k + 2) % 3];
     double* v_new = P.d_v[(k + 1) % 3];

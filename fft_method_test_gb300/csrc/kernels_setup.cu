@@ -252,6 +252,7 @@ static double host_sinc(double x) {
 }
 
 cudaError_t launch_green(Problem& P, double* g64, float* g32) {
+    DeviceMemGuard mem_guard;
     const int Pr = P.p_radius < 0 ? 0 : P.p_radius;
     const int nw = 2 * Pr + 2;
     const double kPi = 3.14159265358979323846;

@@ -72,7 +72,7 @@ def gaussian_field(n, corr_len: float, porosity: float, seed: int):
     ky = np.fft.fftfreq(shape[1])[None, :, None]
     kx = np.fft.rfftfreq(shape[2])[None, None, :]
     filt = np.exp(-2.0 * np.pi ** 2 * corr_len ** 2 * (kx ** 2 + ky ** 2 + kz ** 2))
-    field = np.fft.irfftn(spec * filt, s=shape)
+    field = np.fft.irfftn(spec * filt, s=shape, axes=(0, 1, 2))
     flat = field.ravel()
     k = int(round(porosity * flat.size))
     fluid = np.zeros(flat.size, dtype=np.uint8)

@@ -99,6 +99,12 @@ class PermeabilityProblem:
     def set_precision(self, precision: str):
         self._check(self.lib.fp_set_precision(self._h, PRECISIONS[precision]))
 
+    def autotune(self) -> dict:
+        """fp_autotune: picks the fastest y/z-pass tiling for this grid."""
+        tile, off, ms = C.c_int(0), C.c_int(0), C.c_double(0.0)
+        self._check(self.lib.fp_autotune(self._h, C.byref(tile), C.byref(off), C.byref(ms)))
+        return dict(tile=tile.value, tma=not off.value, apply_ms=ms.value)
+
     def set_geometry(self, fluid_mask: np.ndarray, support: str = "interface") -> int:
         m = np.ascontiguousarray(fluid_mask, dtype=np.uint8)
         if m.shape != self.shape:
@@ -107,6 +113,7 @@ class PermeabilityProblem:
         self._check(self.lib.fp_set_geometry(self._h, m.ravel(), SUPPORT_MODES[support],
                                              C.byref(nb)))
         self.nb = int(nb.value)
+        self.mask = m
         return self.nb
 
     def support(self) -> np.ndarray:
@@ -444,4 +451,62 @@ def computePermeabilityTensorFixedPoint(ids: np.ndarray, fluid_id: int = 1, flui
                                           K, stats)
     _brinkman_check(lib, rc)
     return K.reshape(3, 3), [s.as_dict() for s in stats]
+
+
+def batch_solve_permeability(masks, precision: str = "mixed", tol: float = 1e-7,
+                             maxit: int = 20000, concurrency: int = 4, autotune: bool = True,
+                             voxel_sizes=None, mu: float = 1.0, p_radius: int = 2,
+                             support_mode: int = 0):
+    """fp_batch_solve_permeability over a list of fluid masks (each (nz, ny, nx),
+    sizes may differ): returns (K of shape (count, 3, 3), stats per problem
+    [3 dicts each], status codes)."""
+    lib = _capi.load()
+    count = len(masks)
+    arrs = [np.ascontiguousarray(m, dtype=np.uint8) for m in masks]
+    dims = np.array([[a.shape[2], a.shape[1], a.shape[0]] for a in arrs], dtype=np.int32).ravel()
+    ptrs = (C.c_void_p * max(count, 1))(*[a.ctypes.data for a in arrs])
+    vs = None if voxel_sizes is None else np.ascontiguousarray(voxel_sizes, dtype=np.float64)
+    K = np.zeros(9 * max(count, 1))
+    stats = (_capi.SolverStats * (3 * max(count, 1)))()
+    status = np.zeros(max(count, 1), dtype=np.int32)
+    rc = lib.fp_batch_solve_permeability(count, dims.ctypes.data, ptrs,
+                                         None if vs is None else vs.ctypes.data, float(mu),
+                                         int(p_radius), PRECISIONS[precision], int(support_mode),
+                                         float(tol), int(maxit), int(concurrency), int(autotune),
+                                         K, stats, status.ctypes.data)
+    if rc != _capi.FP_OK:
+        msg = lib.fp_batch_last_error().decode()
+        if rc == _capi.FP_ERR_INVALID:
+            raise ValueError(msg)
+        raise _capi.FpError(rc, msg)
+    st = [[stats[3 * i + c].as_dict() for c in range(3)] for i in range(count)]
+    return K[: 9 * count].reshape(count, 3, 3), st, status[:count].tolist()
+
+
+def write_fvel(path: str, velocity, porosity: float, viscosity: float, driving) -> None:
+    """The reference's .fvel file (fp_write_fvel) from a (3, nz, ny, nx) field."""
+    lib = _capi.load()
+    v = np.asarray(velocity, dtype=np.float64)
+    if v.ndim != 4 or v.shape[0] != 3:
+        raise ValueError("velocity must have shape (3, nz, ny, nx)")
+    nz, ny, nx = v.shape[1:]
+    comps = [np.ascontiguousarray(v[c]).ravel() for c in range(3)]
+    rc = lib.fp_write_fvel(path.encode(), int(nx), int(ny), int(nz), float(porosity),
+                           float(viscosity), np.asarray(driving, np.float64), *comps)
+    if rc != _capi.FP_OK:
+        raise OSError("cannot write velocity file: " + path)
+
+
+def read_fvel(path: str) -> dict:
+    """Reads a .fvel file: dict(velocity (3, nz, ny, nx), porosity, viscosity, driving)."""
+    raw = open(path, "rb").read()
+    if raw[:4] != b"FVEL" or raw[4] != 1:
+        raise ValueError("not a version-1 .fvel file: " + path)
+    nx, ny, nz = np.frombuffer(raw, "<u8", 3, 8)
+    por, mu = np.frombuffer(raw, "<f8", 2, 32)
+    drv = np.frombuffer(raw, "<f8", 3, 48)
+    n = int(nx) * int(ny) * int(nz)
+    rec = np.frombuffer(raw, "<f8", 3 * n, 72).reshape(n, 3)
+    vel = rec.T.reshape(3, int(nz), int(ny), int(nx)).copy()
+    return dict(velocity=vel, porosity=float(por), viscosity=float(mu), driving=drv.copy())
 

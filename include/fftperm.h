@@ -150,6 +150,74 @@ int fp_solve_permeability(fp_handle h, double tol, int64_t maxit, double K[9],
 int fp_green_apply_noalloc(int nx, int ny, int nz, double voxel_size, double mu, int p_radius,
                            const double* d_force_soa, double* d_velocity_soa, void* stream);
 
+/* The reference's .fvel velocity file (write_velocity_field_binary,
+ * src/app/PermeabilityRunner.cpp:109-159) from SoA host fields of N doubles
+ * each (for example the field of fp_recover).  FP_ERR_INVALID when the file
+ * cannot be written. */
+int fp_write_fvel(const char* path, int nx, int ny, int nz, double porosity, double viscosity,
+                  const double driving[3], const double* vx, const double* vy, const double* vz);
+
+/* ---- batches and tuning (no reference counterpart) --------------------------- */
+
+/* Times the operator apply of this handle for each y/z-pass tiling (kx
+ * columns per CTA in {4, 8, 16, 32}, TMA-fed or register-fed) and keeps the
+ * fastest; the choice is cached per (grid, precision) for the process and
+ * applied to later fp_autotune calls on the same grid without timing.
+ * Tiling changes the schedule and the grouping of partial sums (results equal
+ * to rounding).  Outputs may be NULL. */
+int fp_autotune(fp_handle h, int* tile, int* tma_off, double* apply_ms);
+
+/* Permeability tensors of `count` independent microstructures (the reference
+ * runs PermeabilityRunner once per geometry).  Problem i has grid dims[3i..3i+2]
+ * = (nx, ny, nz), fluid mask masks[i] (nz*ny*nx bytes, x fastest) and voxel
+ * size voxel_sizes[i] (NULL: 1).  `concurrency` host threads each solve one
+ * problem at a time on its own handle and stream, largest grids first, so
+ * the problems overlap on the GPU.  autotune != 0 tunes each distinct grid
+ * once first (fp_autotune).  K receives 9 doubles per problem (row-major, as
+ * fp_solve_permeability), stats 3 per problem (may be NULL), status one code
+ * per problem (may be NULL).  Returns the first failing problem's code;
+ * message: fp_batch_last_error(). */
+int fp_batch_solve_permeability(int count, const int* dims, const uint8_t* const* masks,
+                                const double* voxel_sizes, double mu, int p_radius, int precision,
+                                int support_mode, double tol, int64_t maxit, int concurrency,
+                                int autotune, double* K, fp_solver_stats* stats, int* status);
+const char* fp_batch_last_error(void);
+
+/* ---- learned warm start kernels (no reference counterpart) ------------------- */
+/* Building blocks of the warm-start network, all device pointers, queued on
+ * `stream` (cudaStream_t, NULL = legacy default).  Activations are
+ * channels-last BF16 [voxel][channel] over `total` voxels (samples stacked,
+ * each nx*ny*nz, x fastest); weights BF16 [27 taps][cout][cin], tap =
+ * (dz+1)*9 + (dy+1)*3 + (dx+1) times `dilation`, periodic.  The MINRES
+ * initial guess they produce enters through fp_solve_load_case's x0, the
+ * reference's MinresSolver::solve initial_guess (src/solver/MinresSolver.hpp:23).
+ *
+ * fp_nn_conv: y = conv(x) (+ bias, ReLU) for sign +1; for sign -1 and the
+ *   per-tap transposed weights [27][cin_fwd][cout_fwd], the data gradient.
+ *   cin % 16 == 0; cout in {8, 16, 32, 64}; FP32 and/or BF16 output.
+ * fp_nn_wgrad: dW FP32 [27][cout][cin] from dy and x; `partial` is scratch of
+ *   ceil(total/chunk) * 27 * round_up(cout, 16) * cin floats, chunk % 16 == 0.
+ * fp_nn_bias_grad: db[o] = sum_v dy[v][o].
+ * fp_nn_relu_back: BF16 dpre[v][0..cpad) = dpost * (post > 0), zero-padded.
+ * fp_nn_adam: one Adam step on FP32 masters, refreshing the BF16 forward and
+ *   transposed weights.
+ * fp_nn_loss: per-sample relative squared error of the predicted force on
+ *   the support after per-component mean removal, and its gradient. */
+int fp_nn_conv(int nx, int ny, int nz, int64_t total, int dilation, int sign, const void* in_bf16,
+               int cin, const void* w_bf16, const float* bias, int cout, int relu, float* out_f32,
+               void* out_bf16, void* stream);
+int fp_nn_wgrad(int nx, int ny, int nz, int64_t total, int dilation, const void* dy_bf16, int cout,
+                const void* x_bf16, int cin, int64_t chunk, float* partial, float* dw, void* stream);
+int fp_nn_bias_grad(const void* dy_bf16, int64_t total, int cout, float* db, void* stream);
+int fp_nn_relu_back(const float* dpost, const void* post_bf16, int64_t total, int c, int cpad,
+                    void* out_bf16, void* stream);
+int fp_nn_adam(float* w, float* m1, float* m2, const float* g, int64_t count, float lr, float b1,
+               float b2, float eps, float c1, float c2, int cout, int cin, void* wf_bf16,
+               void* wt_bf16, void* stream);
+int fp_nn_loss(const float* pred, int cstride, const float* tgt, const uint8_t* support, int64_t n,
+               int samples, const float* tnorm, float* stats, float* dpred, float* loss,
+               void* stream);
+
 /* ---- Brinkman penalisation (src/brinkman/FluidBrinkman.cpp) ---------------- */
 
 typedef struct fp_brinkman_stats {

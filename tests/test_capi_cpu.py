@@ -4,6 +4,8 @@ import ctypes as C
 import os
 import re
 
+import numpy as np
+
 import pytest
 
 from conftest import ROOT
@@ -62,3 +64,26 @@ def test_cpp_adapters_compile_against_reference(precision):
                         "-I" + os.path.join(ref, "include"), "-I" + os.path.join(ROOT, "include"), src],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_fvel_writer_matches_the_reference_layout(tmp_path):
+    """fp_write_fvel writes the reference's .fvel layout
+    (src/app/PermeabilityRunner.cpp:109-159): 72-byte header, AoS doubles.
+    Host code only: no GPU needed."""
+    import struct
+
+    from fft_method_test_gb300.permeability import read_fvel, write_fvel
+
+    rng = np.random.default_rng(5)
+    v = rng.standard_normal((3, 4, 5, 6))
+    path = str(tmp_path / "out_axis1.fvel")
+    write_fvel(path, v, 0.35, 1.5, (1.0, 0.0, 0.0))
+    raw = open(path, "rb").read()
+    assert len(raw) == 72 + 3 * 8 * v[0].size
+    assert raw[:4] == b"FVEL" and raw[4] == 1 and raw[5:8] == b"\0\0\0"
+    assert struct.unpack("<3Q", raw[8:32]) == (6, 5, 4)
+    assert struct.unpack("<5d", raw[32:72]) == (0.35, 1.5, 1.0, 0.0, 0.0)
+    first = struct.unpack("<3d", raw[72:96])
+    assert first == (v[0, 0, 0, 0], v[1, 0, 0, 0], v[2, 0, 0, 0])
+    r = read_fvel(path)
+    assert np.array_equal(r["velocity"], v) and r["porosity"] == 0.35
