@@ -60,7 +60,7 @@ def parse():
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--mode", default="solve", choices=["solve", "apply", "batch"],
+    ap.add_argument("--mode", default="solve", choices=["solve", "apply", "batch", "learned"],
                     help="apply: only run --reps operator applies per precision (for profilers)")
     ap.add_argument("--precision", default="mixed,fp64", help="precisions for --mode apply")
     ap.add_argument("--reps", type=int, default=3)
@@ -493,8 +493,56 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def run_learned(args):
+    """The learned warm start: train on solver-generated 32^3 pairs, then
+    solve cells from zero and from the network's scaled guess (mixed,
+    tol 1e-7).  Reports training cost, initial residuals and iterations."""
+    import torch
+
+    from fft_method_test_gb300 import geometry as G
+    from fft_method_test_gb300 import learned as L
+    from fft_method_test_gb300.permeability import PermeabilityProblem
+
+    t0 = time.perf_counter()
+    data = L.make_training_set(384, n=32, seed=10000)
+    t_data = time.perf_counter() - t0
+    val = L.make_training_set(8, n=32, seed=20000)
+    net = L.WarmStartNet(seed=0)
+    t0 = time.perf_counter()
+    hist = L.train(net, data, epochs=60, batch=8, lr=2e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    cells = {"grf64_phi0.35_l6_seed30001": G.gaussian_field(64, 6.0, 0.35, seed=30001),
+             "grf64_phi0.35_l6_seed30002": G.gaussian_field(64, 6.0, 0.35, seed=30002),
+             "grf256_phi0.35_l6_seed1003": workload_mask(256, 1003),
+             "grf256_phi0.25_l6_seed20000": G.gaussian_field(256, 6.0, 0.25, seed=20000)}
+    res = {}
+    for name, m in cells.items():
+        rows = []
+        with PermeabilityProblem(m.shape, precision="mixed") as p:
+            p.set_geometry(m)
+            for d in range(3):
+                g = np.zeros(3)
+                g[d] = 1.0
+                _, s0, _ = p.solve_load_case(g, TOL_MIXED, MAXIT)
+                _, s1, used, rel0 = L.solve_load_case_warm(p, net, d, TOL_MIXED, MAXIT)
+                rows.append({"zero_start_iterations": s0["iterations"],
+                             "warm_start_iterations": s1["iterations"], "guess_used": bool(used),
+                             "initial_rel_residual": rel0})
+        res[name] = rows
+    line = {"metric": "learned_warm_start", "data": "synthetic", "n_gpus": 1,
+            "training": {"pairs": len(data), "grid": 32, "epochs": 60, "data_seconds": t_data,
+                         "train_seconds": t_train, "final_train_loss": hist[-1],
+                         "val_loss": L.evaluate(net, val)},
+            "cells": res}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.mode == "learned":
+        run_learned(args)
+        return
     if args.mode == "apply":
         run_applies(args)
         return

@@ -18,7 +18,8 @@ src/solver/MinresSolver.cpp:68-70) that its driver never fills.
   converged interface forces for the unit x gradient.
 * Loss: relative squared error of the predicted forces on the support after
   per-component mean removal (the operator's null space).
-* At solve time the guess is kept only if it lowers the initial residual
+* At solve time the guess is scaled by the factor that minimises the initial
+  residual (one operator apply) and kept only if it lowers that residual
   below the zero start's; otherwise MINRES starts from zero, and MINRES
   always judges the final error.
 
@@ -320,15 +321,20 @@ def predict_guess(net: WarmStartNet, mask: np.ndarray, support: np.ndarray, dire
 
 
 def solve_load_case_warm(problem, net: WarmStartNet, direction: int, tol: float, maxit: int):
-    """fp_solve_load_case with the network's guess when it lowers the initial
-    residual, else from zero.  Returns (avg velocity, stats, used_guess, rel0)."""
+    """fp_solve_load_case from the network's guess, scaled by the factor that
+    minimises the initial residual |b - s A x0| (one operator apply); from
+    zero when that does not lower the residual below |b|.  Returns
+    (avg velocity, stats, used_guess, initial relative residual)."""
     grad = np.zeros(3)
     grad[direction] = 1.0
     sup = problem.support()
     x0 = predict_guess(net, problem.mask, sup, direction)
     b = problem.build_rhs(grad)
-    r = b - problem.operator_apply(x0)
-    rel0 = float(np.linalg.norm(r) / np.linalg.norm(b))
-    use = rel0 < 1.0
+    ax = problem.operator_apply(x0)
+    den = float(ax @ ax)
+    scale = float(b @ ax) / den if den > 0 else 0.0
+    x0 *= scale
+    rel0 = float(np.linalg.norm(b - scale * ax) / np.linalg.norm(b))
+    use = scale > 0 and rel0 < 1.0
     avg, st, _ = problem.solve_load_case(grad, tol, maxit, x0=x0 if use else None)
     return avg, st, use, rel0

@@ -255,3 +255,36 @@ def test_brinkman_fixed_point_oracle_is_where_the_reference_scheme_goes(restatem
         errs.append(float(np.abs(u - uk).max()))
     assert errs[0] > errs[1] > errs[2]
     assert errs[2] < 2e-4
+
+
+def test_network_restatement_gradients():
+    """The CPU restatement of the warm-start network (oracle/nn_ref.py) used
+    to check the GPU kernels: its data gradient is the adjoint of its
+    convolution, its weight gradient and loss gradient match finite
+    differences."""
+    import nn_ref as R
+
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((1, 4, 5, 6, 3))
+    w = rng.standard_normal((27, 2, 3))
+    y = rng.standard_normal((1, 4, 5, 6, 2))
+    for dil in (1, 2):
+        lhs = np.sum(R.conv(x, w, dil) * y)
+        assert abs(lhs - np.sum(x * R.conv_data_grad(y, w, dil))) < 1e-10 * abs(lhs) + 1e-10
+        gw = R.conv_weight_grad(y, x, dil)
+        for t, o, i in ((0, 0, 0), (13, 1, 2), (26, 1, 1)):
+            e = np.zeros_like(w)
+            e[t, o, i] = 1e-6
+            fd = (np.sum(R.conv(x, w + e, dil) * y) - np.sum(R.conv(x, w - e, dil) * y)) / 2e-6
+            assert abs(fd - gw[t, o, i]) < 1e-6 * max(1.0, abs(fd))
+    pred = rng.standard_normal((2, 10, 4))
+    sup = rng.random((2, 10)) > 0.3
+    tgt = rng.standard_normal((2, 10, 3)) * sup[..., None]
+    for b in range(2):
+        tgt[b, sup[b]] -= tgt[b, sup[b]].mean(axis=0)
+    loss, d = R.loss_grad(pred, tgt, sup)
+    e = np.zeros_like(pred)
+    e[1, np.flatnonzero(sup[1])[0], 2] = 1e-6
+    fd = (R.loss_grad(pred + e, tgt, sup)[0][1] - R.loss_grad(pred - e, tgt, sup)[0][1]) / 2e-6
+    assert abs(fd - d[1, np.flatnonzero(sup[1])[0], 2]) < 1e-6
+    assert R.bf16(np.array([1.0, 1.0 + 2 ** -9, 3.0])).tolist() == [1.0, 1.0, 3.0]
