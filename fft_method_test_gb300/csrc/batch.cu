@@ -74,11 +74,11 @@ int time_apply(Problem& P, int reps, double* ms) {
         a.src_kind = kSrcCompact;
         a.dst_kind = kDstCompact;
     } else {
-        DeviceMemGuard mem_guard;
-        if (!P.d_dense_in && cudaMalloc(&P.d_dense_in, sizeof(double) * 3 * (size_t)P.n) != cudaSuccess)
+        if (!P.d_dense_in && cudaMallocAsync(reinterpret_cast<void**>(&P.d_dense_in),
+                                             sizeof(double) * 3 * (size_t)P.n, P.stream) != cudaSuccess)
             return FP_ERR_NOMEM;
-        if (!P.d_dense_out &&
-            cudaMalloc(&P.d_dense_out, sizeof(double) * 3 * (size_t)P.n) != cudaSuccess)
+        if (!P.d_dense_out && cudaMallocAsync(reinterpret_cast<void**>(&P.d_dense_out),
+                                              sizeof(double) * 3 * (size_t)P.n, P.stream) != cudaSuccess)
             return FP_ERR_NOMEM;
         cudaMemsetAsync(P.d_dense_in, 0, sizeof(double) * 3 * (size_t)P.n, P.stream);
         a.src = P.d_dense_in;
@@ -102,7 +102,8 @@ int time_apply(Problem& P, int reps, double* ms) {
     cudaEventDestroy(e1);
     if (err != cudaSuccess) return FP_ERR_CUDA;
     int herr = 0;
-    cudaMemcpy(&herr, P.d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaMemcpyAsync(&herr, P.d_err, sizeof(int), cudaMemcpyDeviceToHost, P.stream);
+    cudaStreamSynchronize(P.stream);
     if (herr) return FP_ERR_CUDA;
     *ms = (double)t / reps;
     return FP_OK;

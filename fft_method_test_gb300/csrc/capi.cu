@@ -11,7 +11,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
+#include <set>
 #include <shared_mutex>
 #include <string>
 #include <vector>
@@ -38,6 +40,51 @@ fp::CaptureGuard::~CaptureGuard() { g_device_mem_mu.unlock_shared(); }
 
 namespace {
 
+// Pinned scalar blocks are reused across handles: cudaFreeHost synchronises
+// the device, so handles hand their block back instead of freeing it.
+std::mutex g_pinned_mu;
+std::vector<fp::MinresScalars*> g_pinned_free;
+
+fp::MinresScalars* take_pinned() {
+    {
+        std::lock_guard<std::mutex> lock(g_pinned_mu);
+        if (!g_pinned_free.empty()) {
+            fp::MinresScalars* p = g_pinned_free.back();
+            g_pinned_free.pop_back();
+            return p;
+        }
+    }
+    fp::DeviceMemGuard mem_guard;
+    void* p = nullptr;
+    if (cudaMallocHost(&p, sizeof(fp::MinresScalars)) != cudaSuccess) return nullptr;
+    return static_cast<fp::MinresScalars*>(p);
+}
+
+void give_pinned(fp::MinresScalars* p) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lock(g_pinned_mu);
+    g_pinned_free.push_back(p);
+}
+
+// Freed stream-ordered memory stays in the device's default pool for the
+// next handle instead of going back to the driver at each synchronisation.
+void keep_pool_memory(int dev) {
+    static std::mutex mu;
+    static std::set<int> done;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.count(dev)) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t threshold = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+    }
+    done.insert(dev);
+}
+
+}  // namespace
+
+namespace {
+
 using fp::Problem;
 
 int fail(Problem& P, int code, const std::string& msg) {
@@ -56,25 +103,32 @@ int cuda_fail(Problem& P, cudaError_t e, const char* where) {
         if (e_ != cudaSuccess) return cuda_fail(P, e_, where); \
     } while (0)
 
+// Device buffers of a handle are stream-ordered allocations on its stream:
+// unlike cudaMalloc / cudaFree they do not synchronise the whole device, so
+// handles on other streams (a batch) keep running through one handle's
+// set-up and tear-down.
 template <typename T>
-cudaError_t dalloc(T** p, size_t count) {
-    return cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * (count > 0 ? count : 1));
+cudaError_t dalloc(Problem& P, T** p, size_t count) {
+    return cudaMallocAsync(reinterpret_cast<void**>(p), sizeof(T) * (count > 0 ? count : 1), P.stream);
+}
+
+void dfree(Problem& P, void* p) {
+    if (p) cudaFreeAsync(p, P.stream);
 }
 
 void free_geometry(Problem& P) {
-    fp::DeviceMemGuard mem_guard_;
     fp::release_graphs(P);
-    cudaFree(P.d_support);
-    cudaFree(P.d_cin);
-    cudaFree(P.d_cout);
-    cudaFree(P.d_b);
-    cudaFree(P.d_x);
-    cudaFree(P.d_z);
-    cudaFree(P.d_r0);
-    cudaFree(P.d_corr);
+    dfree(P, P.d_support);
+    dfree(P, P.d_cin);
+    dfree(P, P.d_cout);
+    dfree(P, P.d_b);
+    dfree(P, P.d_x);
+    dfree(P, P.d_z);
+    dfree(P, P.d_r0);
+    dfree(P, P.d_corr);
     P.d_r0 = P.d_corr = nullptr;
-    for (auto& v : P.d_v) cudaFree(v), v = nullptr;
-    for (auto& w : P.d_w) cudaFree(w), w = nullptr;
+    for (auto& v : P.d_v) dfree(P, v), v = nullptr;
+    for (auto& w : P.d_w) dfree(P, w), w = nullptr;
     P.d_support = nullptr;
     P.d_cin = nullptr;
     P.d_cout = P.d_b = P.d_x = P.d_z = nullptr;
@@ -92,30 +146,29 @@ int need_geometry(Problem& P, const char* who) {
 // A TMA pass whose bounded wait gave up leaves the flag set: report it.
 int check_device_error(Problem& P) {
     int e = 0;
-    FP_CUDA(cudaMemcpy(&e, P.d_err, sizeof(int), cudaMemcpyDeviceToHost), "error flag copy");
+    FP_CUDA(cudaMemcpyAsync(&e, P.d_err, sizeof(int), cudaMemcpyDeviceToHost, P.stream),
+            "error flag copy");
+    FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
     if (e) return fail(P, FP_ERR_CUDA, "a TMA wait in an FFT pass timed out");
     return FP_OK;
 }
 
 int alloc_dense(Problem& P) {
-    fp::DeviceMemGuard mem_guard_;
-    if (!P.d_dense_in) FP_CUDA(dalloc(&P.d_dense_in, 3 * (size_t)P.n), "cudaMalloc dense");
-    if (!P.d_dense_out) FP_CUDA(dalloc(&P.d_dense_out, 3 * (size_t)P.n), "cudaMalloc dense");
+    if (!P.d_dense_in) FP_CUDA(dalloc(P, &P.d_dense_in, 3 * (size_t)P.n), "cudaMalloc dense");
+    if (!P.d_dense_out) FP_CUDA(dalloc(P, &P.d_dense_out, 3 * (size_t)P.n), "cudaMalloc dense");
     return FP_OK;
 }
 
 int ensure_green32(Problem& P) {
-    fp::DeviceMemGuard mem_guard_;
     if (P.d_green32) return FP_OK;
-    FP_CUDA(dalloc(&P.d_green32, 6 * (size_t)P.nh), "cudaMalloc green32");
+    FP_CUDA(dalloc(P, &P.d_green32, 6 * (size_t)P.nh), "cudaMalloc green32");
     FP_CUDA(fp::launch_green(P, nullptr, P.d_green32), "green precompute");
     return FP_OK;
 }
 
 int ensure_green64(Problem& P) {
-    fp::DeviceMemGuard mem_guard_;
     if (P.d_green64) return FP_OK;
-    FP_CUDA(dalloc(&P.d_green64, 6 * (size_t)P.nh), "cudaMalloc green64");
+    FP_CUDA(dalloc(P, &P.d_green64, 6 * (size_t)P.nh), "cudaMalloc green64");
     FP_CUDA(fp::launch_green(P, P.d_green64, nullptr), "green precompute");
     return FP_OK;
 }
@@ -123,12 +176,11 @@ int ensure_green64(Problem& P) {
 // Mixed mode needs both tables: FP32 for the Krylov applies, FP64 for the
 // residuals that start and end each refinement segment.  One launch fills both.
 int ensure_green_both(Problem& P) {
-    fp::DeviceMemGuard mem_guard_;
     if (P.d_green32 && P.d_green64) return FP_OK;
     if (P.d_green32) return ensure_green64(P);
     if (P.d_green64) return ensure_green32(P);
-    FP_CUDA(dalloc(&P.d_green64, 6 * (size_t)P.nh), "cudaMalloc green64");
-    FP_CUDA(dalloc(&P.d_green32, 6 * (size_t)P.nh), "cudaMalloc green32");
+    FP_CUDA(dalloc(P, &P.d_green64, 6 * (size_t)P.nh), "cudaMalloc green64");
+    FP_CUDA(dalloc(P, &P.d_green32, 6 * (size_t)P.nh), "cudaMalloc green32");
     FP_CUDA(fp::launch_green(P, P.d_green64, P.d_green32), "green precompute");
     return FP_OK;
 }
@@ -216,19 +268,18 @@ int read_scalars(Problem& P) {
 // Every P.reliable_interval iterations the segment's own true residual
 // |r0 - A32 (x - x0)| is recomputed (reliable update).  A segment ends when
 // the recurrence reports convergence or breakdown, when that true residual is
-// below tol, or when the recurrence estimate has run ahead of it (below a
-// quarter of it).  The FP64 residual |b - A x| then decides: below tol the
-// solve has converged, otherwise a new segment starts from x.  The reported
+// below tol, or when the recurrence estimate has run ahead of it (below
+// P.ahead_factor = 0.85 of it).  The FP64 residual |b - A x| then decides:
+// below tol the solve has converged, otherwise a new segment starts from x.  The reported
 // residual is that FP64 residual; the history holds the last segment.
 int device_minres(Problem& P, const double* d_b, const double* d_x0, double tol, long long maxit,
                   double* hist_host, fp_solver_stats* st) {
     if (!(tol > 0.0)) return fail(P, FP_ERR_INVALID, "MinresSolver tolerance must be positive");
     if (maxit + 1 > P.hist_cap) {
-        fp::DeviceMemGuard mem_guard_;
         fp::release_graphs(P);  // the graphs write the history through the old pointer
-        cudaFree(P.d_hist);
+        dfree(P, P.d_hist);
         P.d_hist = nullptr;
-        FP_CUDA(dalloc(&P.d_hist, (size_t)maxit + 1), "cudaMalloc hist");
+        FP_CUDA(dalloc(P, &P.d_hist, (size_t)maxit + 1), "cudaMalloc hist");
         P.hist_cap = maxit + 1;
     }
     const bool mixed = P.precision == fp::kMixed && P.reliable_interval > 0;
@@ -281,7 +332,8 @@ int device_minres(Problem& P, const double* d_b, const double* d_x0, double tol,
             int rc = residual_norm(P, P.d_r0, y, fp::kMixed, s.rhs_norm, &seg_rel);
             if (rc) return rc;
         }
-        const bool seg_end = s.done || seg_rel <= tol || s.rel_res < 0.25 * seg_rel;
+        const bool seg_end =
+            s.done || seg_rel <= P.segment_tol_factor * tol || s.rel_res < P.ahead_factor * seg_rel;
         if (!seg_end) continue;
         int rc = residual_norm(P, d_b, P.d_x, fp::kFP64, s.rhs_norm, &rel64);
         if (rc) return rc;
@@ -306,9 +358,10 @@ int device_minres(Problem& P, const double* d_b, const double* d_x0, double tol,
         if (erc) return erc;
     }
     if (hist_host) {
-        FP_CUDA(cudaMemcpy(hist_host, P.d_hist, sizeof(double) * (size_t)(s.it + 1),
-                           cudaMemcpyDeviceToHost),
+        FP_CUDA(cudaMemcpyAsync(hist_host, P.d_hist, sizeof(double) * (size_t)(s.it + 1),
+                                cudaMemcpyDeviceToHost, P.stream),
                 "hist copy");
+        FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
     }
     if (st) {
         st->iterations = done_its + s.it;
@@ -378,7 +431,6 @@ int fp_create(int nx, int ny, int nz, double voxel_size, double mu, int p_radius
 
 int fp::create_handle(int nx, int ny, int nz, double voxel_size, double mu, int p_radius,
                       int precision, bool with_green, fp_handle* out) {
-    fp::DeviceMemGuard mem_guard_;
     if (!out) return FP_ERR_INVALID;
     *out = nullptr;
     fp_problem* h = new (std::nothrow) fp_problem();
@@ -408,24 +460,34 @@ int fp::create_handle(int nx, int ny, int nz, double voxel_size, double mu, int 
     FP_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
     FP_CUDA(cudaDeviceGetAttribute(&P.sm_count, cudaDevAttrMultiProcessorCount, dev), "attr");
     FP_CUDA(cudaStreamCreateWithFlags(&P.stream, cudaStreamNonBlocking), "stream");
+    keep_pool_memory(dev);
     if (const char* t = std::getenv("FFTPERM_TILE_YZ")) P.tile_yz = std::atoi(t);
     if (const char* t = std::getenv("FFTPERM_NO_TMA")) P.tma_off = std::atoi(t) != 0;
     if (const char* t = std::getenv("FFTPERM_NO_GRAPHS")) P.use_graphs = std::atoi(t) == 0;
+    if (const char* t = std::getenv("FFTPERM_AHEAD")) {
+        const double f = std::atof(t);
+        if (f > 0.0 && f < 1.0) P.ahead_factor = f;
+    }
+    if (const char* t = std::getenv("FFTPERM_SEGMENT_TOL")) {
+        const double f = std::atof(t);
+        if (f > 0.0 && f <= 1.0) P.segment_tol_factor = f;
+    }
     std::string err;
-    if (!fp::make_axis_plan(nx, P.px, err) || !fp::make_axis_plan(ny, P.py, err) ||
-        !fp::make_axis_plan(nz, P.pz, err))
+    if (!fp::make_axis_plan(nx, P.px, err, P.stream) || !fp::make_axis_plan(ny, P.py, err, P.stream) ||
+        !fp::make_axis_plan(nz, P.pz, err, P.stream))
         return fail(P, FP_ERR_UNSUPPORTED, err);
-    FP_CUDA(dalloc(reinterpret_cast<double2**>(&P.d_spec), 3 * (size_t)P.nh), "cudaMalloc spec");
+    FP_CUDA(dalloc(P, reinterpret_cast<double2**>(&P.d_spec), 3 * (size_t)P.nh), "cudaMalloc spec");
     const size_t nparts = (size_t)std::max<long long>(fp::kMaxPartials, P.nrows + 64);
-    FP_CUDA(dalloc(&P.d_partials, 4 * nparts), "cudaMalloc partials");
-    FP_CUDA(dalloc(&P.d_red, 64), "cudaMalloc red");
-    FP_CUDA(dalloc(&P.d_sc, 1), "cudaMalloc scalars");
-    FP_CUDA(dalloc(&P.d_err, 1), "cudaMalloc error flag");
-    FP_CUDA(cudaMemset(P.d_err, 0, sizeof(int)), "memset");
-    FP_CUDA(cudaMallocHost(&P.h_sc, sizeof(fp::MinresScalars)), "cudaMallocHost");
-    FP_CUDA(dalloc(&P.d_row_ptr, (size_t)P.nrows + 1), "cudaMalloc row_ptr");
-    FP_CUDA(dalloc(&P.d_row_cnt, (size_t)P.nrows + 1), "cudaMalloc row_cnt");
-    FP_CUDA(dalloc(&P.d_mask, (size_t)P.n), "cudaMalloc mask");
+    FP_CUDA(dalloc(P, &P.d_partials, 4 * nparts), "cudaMalloc partials");
+    FP_CUDA(dalloc(P, &P.d_red, 64), "cudaMalloc red");
+    FP_CUDA(dalloc(P, &P.d_sc, 1), "cudaMalloc scalars");
+    FP_CUDA(dalloc(P, &P.d_err, 1), "cudaMalloc error flag");
+    FP_CUDA(cudaMemsetAsync(P.d_err, 0, sizeof(int), P.stream), "memset");
+    P.h_sc = take_pinned();
+    if (!P.h_sc) return fail(P, FP_ERR_NOMEM, "cudaMallocHost failed");
+    FP_CUDA(dalloc(P, &P.d_row_ptr, (size_t)P.nrows + 1), "cudaMalloc row_ptr");
+    FP_CUDA(dalloc(P, &P.d_row_cnt, (size_t)P.nrows + 1), "cudaMalloc row_cnt");
+    FP_CUDA(dalloc(P, &P.d_mask, (size_t)P.n), "cudaMalloc mask");
     if (!with_green) return FP_OK;
     int rc = (precision == FP_PREC_MIXED) ? ensure_green_both(P) : ensure_green64(P);
     if (rc) return rc;
@@ -435,28 +497,28 @@ int fp::create_handle(int nx, int ny, int nz, double voxel_size, double mu, int 
 extern "C" {
 
 int fp_destroy(fp_handle h) {
-    fp::DeviceMemGuard mem_guard_;
     if (!h) return FP_OK;
     Problem& P = h->P;
     if (P.stream) cudaStreamSynchronize(P.stream);
     free_geometry(P);
-    fp::free_axis_plan(P.px);
-    fp::free_axis_plan(P.py);
-    fp::free_axis_plan(P.pz);
-    cudaFree(P.d_spec);
-    cudaFree(P.d_green64);
-    cudaFree(P.d_green32);
-    cudaFree(P.d_dense_in);
-    cudaFree(P.d_dense_out);
-    cudaFree(P.d_partials);
-    cudaFree(P.d_red);
-    cudaFree(P.d_sc);
-    cudaFree(P.d_err);
-    cudaFree(P.d_hist);
-    cudaFree(P.d_row_ptr);
-    cudaFree(P.d_row_cnt);
-    cudaFree(P.d_mask);
-    if (P.h_sc) cudaFreeHost(P.h_sc);
+    fp::free_axis_plan(P.px, P.stream);
+    fp::free_axis_plan(P.py, P.stream);
+    fp::free_axis_plan(P.pz, P.stream);
+    dfree(P, P.d_spec);
+    dfree(P, P.d_green64);
+    dfree(P, P.d_green32);
+    dfree(P, P.d_dense_in);
+    dfree(P, P.d_dense_out);
+    dfree(P, P.d_partials);
+    dfree(P, P.d_red);
+    dfree(P, P.d_sc);
+    dfree(P, P.d_err);
+    dfree(P, P.d_hist);
+    dfree(P, P.d_row_ptr);
+    dfree(P, P.d_row_cnt);
+    dfree(P, P.d_mask);
+    give_pinned(P.h_sc);
+    P.h_sc = nullptr;
     if (P.stream) cudaStreamDestroy(P.stream);
     delete h;
     return FP_OK;
@@ -490,7 +552,6 @@ int fp_set_precision(fp_handle h, int precision) {
 }
 
 int fp_set_geometry(fp_handle h, const uint8_t* fluid_mask, int support_mode, int64_t* nb_out) {
-    fp::DeviceMemGuard mem_guard_;
     if (!h) return FP_ERR_INVALID;
     Problem& P = h->P;
     if (!fluid_mask) return fail(P, FP_ERR_INVALID, "BinaryMedium mask must not be null");
@@ -502,15 +563,15 @@ int fp_set_geometry(fp_handle h, const uint8_t* fluid_mask, int support_mode, in
             "mask copy");
     FP_CUDA(fp::launch_support(P), "support");
     const size_t m = 3 * (size_t)P.nb;
-    FP_CUDA(dalloc(&P.d_cin, m), "cudaMalloc");
-    FP_CUDA(dalloc(&P.d_cout, m), "cudaMalloc");
-    FP_CUDA(dalloc(&P.d_b, m), "cudaMalloc");
-    FP_CUDA(dalloc(&P.d_x, m), "cudaMalloc");
-    FP_CUDA(dalloc(&P.d_z, m), "cudaMalloc");
-    FP_CUDA(dalloc(&P.d_r0, m), "cudaMalloc");
-    FP_CUDA(dalloc(&P.d_corr, m), "cudaMalloc");
-    for (auto& v : P.d_v) FP_CUDA(dalloc(&v, m), "cudaMalloc");
-    for (auto& w : P.d_w) FP_CUDA(dalloc(&w, m), "cudaMalloc");
+    FP_CUDA(dalloc(P, &P.d_cin, m), "cudaMalloc");
+    FP_CUDA(dalloc(P, &P.d_cout, m), "cudaMalloc");
+    FP_CUDA(dalloc(P, &P.d_b, m), "cudaMalloc");
+    FP_CUDA(dalloc(P, &P.d_x, m), "cudaMalloc");
+    FP_CUDA(dalloc(P, &P.d_z, m), "cudaMalloc");
+    FP_CUDA(dalloc(P, &P.d_r0, m), "cudaMalloc");
+    FP_CUDA(dalloc(P, &P.d_corr, m), "cudaMalloc");
+    for (auto& v : P.d_v) FP_CUDA(dalloc(P, &v, m), "cudaMalloc");
+    for (auto& w : P.d_w) FP_CUDA(dalloc(P, &w, m), "cudaMalloc");
     FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
     P.has_geometry = true;
     if (nb_out) *nb_out = P.nb;
@@ -522,8 +583,10 @@ int fp_get_support(fp_handle h, int64_t* out) {
     Problem& P = h->P;
     if (!P.has_geometry) return fail(P, FP_ERR_STATE, "fp_get_support: no geometry set");
     std::vector<int> tmp((size_t)P.nb);
-    FP_CUDA(cudaMemcpy(tmp.data(), P.d_support, sizeof(int) * tmp.size(), cudaMemcpyDeviceToHost),
+    FP_CUDA(cudaMemcpyAsync(tmp.data(), P.d_support, sizeof(int) * tmp.size(), cudaMemcpyDeviceToHost,
+                            P.stream),
             "copy");
+    FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
     for (size_t i = 0; i < tmp.size(); ++i) out[i] = tmp[i];
     return FP_OK;
 }
@@ -533,9 +596,11 @@ int fp_get_green(fp_handle h, double* g6) {
     Problem& P = h->P;
     int rc = ensure_green64(P);
     if (rc) return rc;
-    FP_CUDA(cudaMemcpy2D(g6, sizeof(double) * P.nxh, P.d_green64, sizeof(double) * P.rs,
-                         sizeof(double) * P.nxh, 6 * (size_t)P.nrows, cudaMemcpyDeviceToHost),
+    FP_CUDA(cudaMemcpy2DAsync(g6, sizeof(double) * P.nxh, P.d_green64, sizeof(double) * P.rs,
+                              sizeof(double) * P.nxh, 6 * (size_t)P.nrows, cudaMemcpyDeviceToHost,
+                              P.stream),
             "copy");
+    FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
     return FP_OK;
 }
 
@@ -690,9 +755,10 @@ int fp_recover(fp_handle h, const double grad[3], const double* x, double* v_soa
     rc = device_recover(P, grad, P.d_cin, avg, v_soa != nullptr);
     if (rc) return rc;
     if (v_soa) {
-        FP_CUDA(cudaMemcpy(v_soa, P.d_dense_out, sizeof(double) * 3 * (size_t)P.n,
-                           cudaMemcpyDeviceToHost),
+        FP_CUDA(cudaMemcpyAsync(v_soa, P.d_dense_out, sizeof(double) * 3 * (size_t)P.n,
+                                cudaMemcpyDeviceToHost, P.stream),
                 "copy");
+        FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
     }
     return FP_OK;
 }

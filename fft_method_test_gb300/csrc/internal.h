@@ -25,8 +25,9 @@ struct AxisPlan {
 };
 
 // Build a plan for length n (factors 2, 3, 5 only); returns false otherwise.
-bool make_axis_plan(int n, AxisPlan& p, std::string& err);
-void free_axis_plan(AxisPlan& p);
+// Twiddle tables are stream-ordered allocations on the handle's stream.
+bool make_axis_plan(int n, AxisPlan& p, std::string& err, cudaStream_t stream);
+void free_axis_plan(AxisPlan& p, cudaStream_t stream);
 
 // MINRES scalar state on the device (all FP64).  Layout is private.
 struct MinresScalars {
@@ -81,6 +82,12 @@ struct Problem {
     int sm_count = 0;
     int tile_yz = 0;  // kx columns per CTA of the y and z passes (0 = default)
     int reliable_interval = 20;  // mixed precision: true-residual check every this many iterations
+    // mixed precision: a refinement segment ends when the recurrence estimate
+    // falls below this fraction of the segment's true residual
+    double ahead_factor = 0.85;
+    // mixed precision: a segment also ends when its true residual is below
+    // this fraction of tol (then the FP64 residual decides)
+    double segment_tol_factor = 1.0;
 
     AxisPlan px, py, pz;
 

@@ -64,7 +64,7 @@ bool fill_plan_radices(int n, FftPlanDev& d) {
     return true;
 }
 
-bool make_axis_plan(int n, AxisPlan& p, std::string& err) {
+bool make_axis_plan(int n, AxisPlan& p, std::string& err, cudaStream_t stream) {
     p = AxisPlan{};
     if (n > 640) {
         // the FP64 z pass keeps the three components of one column in one
@@ -94,21 +94,22 @@ bool make_axis_plan(int n, AxisPlan& p, std::string& err) {
         h64[j] = make_double2(std::cos(a), -std::sin(a));
         h32[j] = make_float2((float)h64[j].x, (float)h64[j].y);
     }
-    if (cudaMalloc(&p.tw64, sizeof(double2) * n) != cudaSuccess ||
-        cudaMalloc(&p.tw32, sizeof(float2) * n) != cudaSuccess) {
-        err = "cudaMalloc failed for FFT twiddles";
+    if (cudaMallocAsync(reinterpret_cast<void**>(&p.tw64), sizeof(double2) * n, stream) != cudaSuccess ||
+        cudaMallocAsync(reinterpret_cast<void**>(&p.tw32), sizeof(float2) * n, stream) != cudaSuccess) {
+        err = "device allocation failed for FFT twiddles";
         return false;
     }
-    cudaMemcpy(p.tw64, h64.data(), sizeof(double2) * n, cudaMemcpyHostToDevice);
-    cudaMemcpy(p.tw32, h32.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);
+    cudaMemcpyAsync(p.tw64, h64.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(p.tw32, h32.data(), sizeof(float2) * n, cudaMemcpyHostToDevice, stream);
+    cudaStreamSynchronize(stream);  // the host tables must outlive their copies
     p.dev.tw64 = p.tw64;
     p.dev.tw32 = p.tw32;
     return true;
 }
 
-void free_axis_plan(AxisPlan& p) {
-    cudaFree(p.tw64);
-    cudaFree(p.tw32);
+void free_axis_plan(AxisPlan& p, cudaStream_t stream) {
+    if (p.tw64) cudaFreeAsync(p.tw64, stream);
+    if (p.tw32) cudaFreeAsync(p.tw32, stream);
     p.tw64 = nullptr;
     p.tw32 = nullptr;
 }

@@ -252,7 +252,6 @@ static double host_sinc(double x) {
 }
 
 cudaError_t launch_green(Problem& P, double* g64, float* g32) {
-    DeviceMemGuard mem_guard;
     const int Pr = P.p_radius < 0 ? 0 : P.p_radius;
     const int nw = 2 * Pr + 2;
     const double kPi = 3.14159265358979323846;
@@ -274,7 +273,8 @@ cudaError_t launch_green(Problem& P, double* g64, float* g32) {
     tab(P.nz, hsz, hqz);
     const size_t tx = hsx.size(), ty = hsy.size(), tz = hsz.size();
     double* d = nullptr;
-    cudaError_t e = cudaMalloc(&d, sizeof(double) * 2 * (tx + ty + tz));
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&d), sizeof(double) * 2 * (tx + ty + tz),
+                                    P.stream);
     if (e != cudaSuccess) return e;
     double* dsx = d;
     double* dqx = dsx + tx;
@@ -282,12 +282,12 @@ cudaError_t launch_green(Problem& P, double* g64, float* g32) {
     double* dqy = dsy + ty;
     double* dsz = dqy + ty;
     double* dqz = dsz + tz;
-    cudaMemcpy(dsx, hsx.data(), sizeof(double) * tx, cudaMemcpyHostToDevice);
-    cudaMemcpy(dqx, hqx.data(), sizeof(double) * tx, cudaMemcpyHostToDevice);
-    cudaMemcpy(dsy, hsy.data(), sizeof(double) * ty, cudaMemcpyHostToDevice);
-    cudaMemcpy(dqy, hqy.data(), sizeof(double) * ty, cudaMemcpyHostToDevice);
-    cudaMemcpy(dsz, hsz.data(), sizeof(double) * tz, cudaMemcpyHostToDevice);
-    cudaMemcpy(dqz, hqz.data(), sizeof(double) * tz, cudaMemcpyHostToDevice);
+    cudaMemcpyAsync(dsx, hsx.data(), sizeof(double) * tx, cudaMemcpyHostToDevice, P.stream);
+    cudaMemcpyAsync(dqx, hqx.data(), sizeof(double) * tx, cudaMemcpyHostToDevice, P.stream);
+    cudaMemcpyAsync(dsy, hsy.data(), sizeof(double) * ty, cudaMemcpyHostToDevice, P.stream);
+    cudaMemcpyAsync(dqy, hqy.data(), sizeof(double) * ty, cudaMemcpyHostToDevice, P.stream);
+    cudaMemcpyAsync(dsz, hsz.data(), sizeof(double) * tz, cudaMemcpyHostToDevice, P.stream);
+    cudaMemcpyAsync(dqz, hqz.data(), sizeof(double) * tz, cudaMemcpyHostToDevice, P.stream);
     GreenArgs a{};
     a.nx = P.nx;
     a.ny = P.ny;
@@ -307,8 +307,8 @@ cudaError_t launch_green(Problem& P, double* g64, float* g32) {
     a.g32 = g32;
     a.nh = P.nh;
     e = launch_green_kernel(a, P.stream);
-    cudaStreamSynchronize(P.stream);
-    cudaFree(d);
+    cudaFreeAsync(d, P.stream);
+    cudaStreamSynchronize(P.stream);  // the host tables above must outlive their copies
     return e;
 }
 
