@@ -12,7 +12,8 @@
 // taken largest first, which keeps the tail of the batch short.
 //
 // Autotuner.  The y and z passes take `tile` kx columns per CTA and have a
-// TMA-fed and a register-fed variant.  fp_autotune times the operator apply
+// TMA-fed and a register-fed variant; the inverse x pass has a bulk-copy
+// pipelined and a one-tile-per-CTA variant.  fp_autotune times the operator apply
 // of a handle for each candidate and keeps the fastest; results are cached per
 // (grid, precision) for the process.  The batch tunes every distinct grid
 // once before the workers start, so that the timings see an idle GPU.
@@ -46,6 +47,7 @@ struct TuneKey {
 struct TuneResult {
     int tile = 0;
     bool tma_off = false;
+    bool x_bulk = true;
     double ms = 0.0;
 };
 
@@ -54,11 +56,12 @@ std::map<TuneKey, TuneResult> g_tune_cache;
 
 thread_local std::string g_batch_error;
 
-void apply_tiling(Problem& P, int tile, bool tma_off) {
-    if (P.tile_yz == tile && P.tma_off == tma_off) return;
+void apply_tiling(Problem& P, int tile, bool tma_off, bool x_bulk) {
+    if (P.tile_yz == tile && P.tma_off == tma_off && P.x_bulk == x_bulk) return;
     release_graphs(P);
     P.tile_yz = tile;
     P.tma_off = tma_off;
+    P.x_bulk = x_bulk;
     for (auto& c : P.tma_y) c.valid = false;
     for (auto& c : P.tma_z) c.valid = false;
 }
@@ -116,32 +119,36 @@ int tune(Problem& P, TuneResult* out) {
         auto it = g_tune_cache.find(key);
         if (it != g_tune_cache.end()) {
             *out = it->second;
-            apply_tiling(P, out->tile, out->tma_off);
+            apply_tiling(P, out->tile, out->tma_off, out->x_bulk);
             return FP_OK;
         }
     }
     const int tile0 = P.tile_yz;
     const bool tma0 = P.tma_off;
+    const bool bulk0 = P.x_bulk;
     TuneResult best;
     best.ms = 1e30;
     const int tiles[] = {4, 8, 16, 32};
-    for (int off = 0; off < 2; ++off) {
-        for (int t : tiles) {
-            apply_tiling(P, t, off != 0);
-            double ms = 0.0;
-            const int rc = time_apply(P, 3, &ms);
-            if (rc != FP_OK) {
-                apply_tiling(P, tile0, tma0);
-                return rc;
-            }
-            if (ms < best.ms) {
-                best.ms = ms;
-                best.tile = t;
-                best.tma_off = off != 0;
+    for (int xb = 0; xb < 2; ++xb) {
+        for (int off = 0; off < 2; ++off) {
+            for (int t : tiles) {
+                apply_tiling(P, t, off != 0, xb == 0);
+                double ms = 0.0;
+                const int rc = time_apply(P, 3, &ms);
+                if (rc != FP_OK) {
+                    apply_tiling(P, tile0, tma0, bulk0);
+                    return rc;
+                }
+                if (ms < best.ms) {
+                    best.ms = ms;
+                    best.tile = t;
+                    best.tma_off = off != 0;
+                    best.x_bulk = xb == 0;
+                }
             }
         }
     }
-    apply_tiling(P, best.tile, best.tma_off);
+    apply_tiling(P, best.tile, best.tma_off, best.x_bulk);
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         g_tune_cache[key] = best;

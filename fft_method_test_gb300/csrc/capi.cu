@@ -462,7 +462,10 @@ int fp::create_handle(int nx, int ny, int nz, double voxel_size, double mu, int 
     FP_CUDA(cudaStreamCreateWithFlags(&P.stream, cudaStreamNonBlocking), "stream");
     keep_pool_memory(dev);
     if (const char* t = std::getenv("FFTPERM_TILE_YZ")) P.tile_yz = std::atoi(t);
-    if (const char* t = std::getenv("FFTPERM_NO_TMA")) P.tma_off = std::atoi(t) != 0;
+    if (const char* t = std::getenv("FFTPERM_NO_TMA")) {
+        P.tma_off = std::atoi(t) != 0;  // every TMA / bulk-copy pass off
+        P.x_bulk = !P.tma_off;
+    }
     if (const char* t = std::getenv("FFTPERM_NO_GRAPHS")) P.use_graphs = std::atoi(t) == 0;
     if (const char* t = std::getenv("FFTPERM_AHEAD")) {
         const double f = std::atof(t);

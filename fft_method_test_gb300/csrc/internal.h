@@ -140,6 +140,7 @@ struct Problem {
     MinresGraph graphs[6];
     long long queued = 0;  // iterations queued since minres_start (buffer rotation)
     bool tma_off = false;      // FFTPERM_NO_TMA=1 selects the register-fed passes
+    bool x_bulk = true;        // inverse x pass fed by bulk copies (tuned)
     int* d_err = nullptr;      // device error flag (a bounded wait gave up)
 
     std::string err;

@@ -352,7 +352,7 @@ static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     XArgs xb = x;
     int raw_bytes = 0;
     size_t bsmem = 0;
-    bool bulk = !P.tma_off && P.d_err;
+    bool bulk = P.x_bulk && P.d_err;
     if (bulk) {
         for (;;) {
             const int nqb = (3 * xb.rows_per_cta + 1) / 2;

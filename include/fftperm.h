@@ -160,7 +160,8 @@ int fp_write_fvel(const char* path, int nx, int ny, int nz, double porosity, dou
 /* ---- batches and tuning (no reference counterpart) --------------------------- */
 
 /* Times the operator apply of this handle for each y/z-pass tiling (kx
- * columns per CTA in {4, 8, 16, 32}, TMA-fed or register-fed) and keeps the
+ * columns per CTA in {4, 8, 16, 32}, TMA-fed or register-fed) and each
+ * inverse-x variant (bulk-copy pipelined or one tile per CTA), and keeps the
  * fastest; the choice is cached per (grid, precision) for the process and
  * applied to later fp_autotune calls on the same grid without timing.
  * Tiling changes the schedule and the grouping of partial sums (results equal
