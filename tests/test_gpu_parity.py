@@ -340,3 +340,30 @@ def test_mixed_precision_minres_reaches_fp64_tolerance(gpu_lib, restatement):
     true_rel = np.linalg.norm(b - ctx.operator_apply(r.solution)) / np.linalg.norm(b)
     assert true_rel <= 1.05 * tol, true_rel
     assert abs(true_rel - r.final_rel_residual) <= 0.05 * tol
+
+
+def test_largest_grid_512_apply_properties(gpu_lib):
+    """At 512^3 (134 M voxels, beyond any oracle run): the FP64 operator is
+    symmetric to round-off, the mixed (FP32) apply agrees with it to FP32
+    accuracy, and the RHS has zero mean per component."""
+    from fft_method_test_gb300.permeability import PermeabilityProblem
+
+    n = 512
+    z, y, x = np.ogrid[:n, :n, :n]
+    field = (np.sin(2 * np.pi * x / 64) * np.sin(2 * np.pi * y / 128 + 0.3)
+             + np.sin(2 * np.pi * z / 80) * np.cos(2 * np.pi * x / 128))
+    mask = (field < 0.4).astype(np.uint8)
+    del field
+    rng = np.random.default_rng(7)
+    with PermeabilityProblem(mask.shape, precision="fp64") as p:
+        nb = p.set_geometry(mask)
+        a = rng.uniform(-1, 1, 3 * nb)
+        b = rng.uniform(-1, 1, 3 * nb)
+        Aa = p.operator_apply(a)
+        Ab = p.operator_apply(b)
+        assert abs(a @ Ab - b @ Aa) < 1e-11 * np.abs(a) @ np.abs(Ab)
+        rhs = p.build_rhs((0.0, 0.0, 1.0)).reshape(-1, 3)
+        assert np.abs(rhs.mean(axis=0)).max() < 1e-12 * np.abs(rhs).max()
+        p.set_precision("mixed")
+        Aa32 = p.operator_apply(a)
+    assert rel_err(Aa32, Aa) < 5e-6
