@@ -37,7 +37,7 @@ EXPORTED = [
     "fp_solve_load_case", "fp_solve_permeability", "fp_brinkman_solve",
     "fp_brinkman_permeability", "fp_brinkman_last_error", "fp_green_apply_noalloc",
     "fp_kernel_launch_count", "fp_brinkman_fft_solve", "fp_brinkman_fft_permeability",
-    "fp_autotune", "fp_batch_solve_permeability", "fp_batch_last_error", "fp_write_fvel",
+    "fp_autotune", "fp_set_tiling", "fp_batch_solve_permeability", "fp_batch_last_error", "fp_write_fvel",
     "fp_nn_conv", "fp_nn_wgrad", "fp_nn_bias_grad", "fp_nn_relu_back", "fp_nn_adam", "fp_nn_loss",
 ]
 
@@ -111,7 +111,8 @@ _SIGNATURES = {
                                   C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
                                   C.c_double, _dp, C.POINTER(BrinkmanStats)], C.c_int),
     "fp_brinkman_last_error": ([], C.c_char_p),
-    "fp_autotune": ([_h, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "fp_autotune": ([_h, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "fp_set_tiling": ([_h, C.c_int, C.c_int, C.c_int], C.c_int),
     "fp_batch_solve_permeability": ([C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
                                      C.c_int, C.c_int, C.c_int, C.c_double, C.c_int64, C.c_int,
                                      C.c_int, _dp, C.c_void_p, C.c_void_p], C.c_int),

@@ -165,7 +165,7 @@ struct Job {
 }  // namespace
 }  // namespace fp
 
-extern "C" int fp_autotune(fp_handle h, int* tile, int* tma_off, double* apply_ms) {
+extern "C" int fp_autotune(fp_handle h, int* tile, int* tma_off, int* x_bulk, double* apply_ms) {
     using namespace fp;
     if (!h) return FP_ERR_INVALID;
     TuneResult r;
@@ -176,7 +176,19 @@ extern "C" int fp_autotune(fp_handle h, int* tile, int* tma_off, double* apply_m
     }
     if (tile) *tile = r.tile;
     if (tma_off) *tma_off = r.tma_off ? 1 : 0;
+    if (x_bulk) *x_bulk = r.x_bulk ? 1 : 0;
     if (apply_ms) *apply_ms = r.ms;
+    return FP_OK;
+}
+
+extern "C" int fp_set_tiling(fp_handle h, int tile, int tma_off, int x_bulk) {
+    using namespace fp;
+    if (!h) return FP_ERR_INVALID;
+    if (tile != 0 && tile != 2 && tile != 4 && tile != 8 && tile != 16 && tile != 32) {
+        h->P.err = "fp_set_tiling: tile must be 0 (default), 2, 4, 8, 16 or 32";
+        return FP_ERR_INVALID;
+    }
+    apply_tiling(h->P, tile, tma_off != 0, x_bulk != 0);
     return FP_OK;
 }
 

@@ -100,10 +100,15 @@ class PermeabilityProblem:
         self._check(self.lib.fp_set_precision(self._h, PRECISIONS[precision]))
 
     def autotune(self) -> dict:
-        """fp_autotune: picks the fastest y/z-pass tiling for this grid."""
-        tile, off, ms = C.c_int(0), C.c_int(0), C.c_double(0.0)
-        self._check(self.lib.fp_autotune(self._h, C.byref(tile), C.byref(off), C.byref(ms)))
-        return dict(tile=tile.value, tma=not off.value, apply_ms=ms.value)
+        """fp_autotune: picks the fastest FFT tiling for this grid."""
+        tile, off, xb, ms = C.c_int(0), C.c_int(0), C.c_int(0), C.c_double(0.0)
+        self._check(self.lib.fp_autotune(self._h, C.byref(tile), C.byref(off), C.byref(xb),
+                                         C.byref(ms)))
+        return dict(tile=tile.value, tma=not off.value, x_bulk=bool(xb.value), apply_ms=ms.value)
+
+    def set_tiling(self, tile: int = 0, tma: bool = True, x_bulk: bool = True):
+        """fp_set_tiling: a given FFT tiling (e.g. one autotune reported)."""
+        self._check(self.lib.fp_set_tiling(self._h, int(tile), int(not tma), int(x_bulk)))
 
     def set_geometry(self, fluid_mask: np.ndarray, support: str = "interface") -> int:
         m = np.ascontiguousarray(fluid_mask, dtype=np.uint8)

@@ -95,3 +95,23 @@ def test_batch_errors(gpu_lib):
         batch_solve_permeability([G.spheres(8, 1.5, 0.6, seed=1)], concurrency=0)
     K, _, status = batch_solve_permeability([], concurrency=2)
     assert K.shape == (0, 3, 3) and status == []
+
+
+def test_set_tiling_reproduces_the_tuned_apply(gpu_lib):
+    """fp_set_tiling with the tuner's report gives the tuned schedule's result."""
+    from fft_method_test_gb300.permeability import PermeabilityProblem
+
+    mask = G.gaussian_field(40, 4.0, 0.4, seed=44)
+    x = None
+    with PermeabilityProblem(mask.shape, precision="mixed") as p:
+        nb = p.set_geometry(mask)
+        x = np.random.default_rng(1).uniform(-1, 1, 3 * nb)
+        t = p.autotune()
+        y0 = p.operator_apply(x)
+    with PermeabilityProblem(mask.shape, precision="mixed") as q:
+        q.set_geometry(mask)
+        q.set_tiling(t["tile"], t["tma"], t["x_bulk"])
+        y1 = q.operator_apply(x)
+        with pytest.raises(Exception):
+            q.set_tiling(7, True, True)
+    assert np.array_equal(y0, y1)
