@@ -13,7 +13,8 @@
 //
 // Autotuner.  The y and z passes take `tile` kx columns per CTA and have a
 // TMA-fed and a register-fed variant; the inverse x pass has a bulk-copy
-// pipelined and a one-tile-per-CTA variant.  fp_autotune times the operator apply
+// pipelined and a one-tile-per-CTA variant; the x passes' rows per CTA can
+// be capped (smaller CTAs, more of them per SM).  fp_autotune times the operator apply
 // of a handle for each candidate and keeps the fastest; results are cached per
 // (grid, precision) for the process.  The batch tunes every distinct grid
 // once before the workers start, so that the timings see an idle GPU.
@@ -48,6 +49,7 @@ struct TuneResult {
     int tile = 0;
     bool tma_off = false;
     bool x_bulk = true;
+    int x_rows = 0;
     double ms = 0.0;
 };
 
@@ -56,12 +58,13 @@ std::map<TuneKey, TuneResult> g_tune_cache;
 
 thread_local std::string g_batch_error;
 
-void apply_tiling(Problem& P, int tile, bool tma_off, bool x_bulk) {
-    if (P.tile_yz == tile && P.tma_off == tma_off && P.x_bulk == x_bulk) return;
+void apply_tiling(Problem& P, int tile, bool tma_off, bool x_bulk, int x_rows) {
+    if (P.tile_yz == tile && P.tma_off == tma_off && P.x_bulk == x_bulk && P.x_rows == x_rows) return;
     release_graphs(P);
     P.tile_yz = tile;
     P.tma_off = tma_off;
     P.x_bulk = x_bulk;
+    P.x_rows = x_rows;
     for (auto& c : P.tma_y) c.valid = false;
     for (auto& c : P.tma_z) c.valid = false;
 }
@@ -119,36 +122,41 @@ int tune(Problem& P, TuneResult* out) {
         auto it = g_tune_cache.find(key);
         if (it != g_tune_cache.end()) {
             *out = it->second;
-            apply_tiling(P, out->tile, out->tma_off, out->x_bulk);
+            apply_tiling(P, out->tile, out->tma_off, out->x_bulk, out->x_rows);
             return FP_OK;
         }
     }
     const int tile0 = P.tile_yz;
     const bool tma0 = P.tma_off;
     const bool bulk0 = P.x_bulk;
+    const int rows0 = P.x_rows;
     TuneResult best;
     best.ms = 1e30;
     const int tiles[] = {4, 8, 16, 32};
-    for (int xb = 0; xb < 2; ++xb) {
-        for (int off = 0; off < 2; ++off) {
-            for (int t : tiles) {
-                apply_tiling(P, t, off != 0, xb == 0);
-                double ms = 0.0;
-                const int rc = time_apply(P, 3, &ms);
-                if (rc != FP_OK) {
-                    apply_tiling(P, tile0, tma0, bulk0);
-                    return rc;
-                }
-                if (ms < best.ms) {
-                    best.ms = ms;
-                    best.tile = t;
-                    best.tma_off = off != 0;
-                    best.x_bulk = xb == 0;
+    const int xrows[] = {0, 4, 2};
+    for (int xr : xrows) {
+        for (int xb = 0; xb < 2; ++xb) {
+            for (int off = 0; off < 2; ++off) {
+                for (int t : tiles) {
+                    apply_tiling(P, t, off != 0, xb == 0, xr);
+                    double ms = 0.0;
+                    const int rc = time_apply(P, 3, &ms);
+                    if (rc != FP_OK) {
+                        apply_tiling(P, tile0, tma0, bulk0, rows0);
+                        return rc;
+                    }
+                    if (ms < best.ms) {
+                        best.ms = ms;
+                        best.tile = t;
+                        best.tma_off = off != 0;
+                        best.x_bulk = xb == 0;
+                        best.x_rows = xr;
+                    }
                 }
             }
         }
     }
-    apply_tiling(P, best.tile, best.tma_off, best.x_bulk);
+    apply_tiling(P, best.tile, best.tma_off, best.x_bulk, best.x_rows);
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         g_tune_cache[key] = best;
@@ -165,7 +173,8 @@ struct Job {
 }  // namespace
 }  // namespace fp
 
-extern "C" int fp_autotune(fp_handle h, int* tile, int* tma_off, int* x_bulk, double* apply_ms) {
+extern "C" int fp_autotune(fp_handle h, int* tile, int* tma_off, int* x_bulk, int* x_rows,
+                           double* apply_ms) {
     using namespace fp;
     if (!h) return FP_ERR_INVALID;
     TuneResult r;
@@ -177,18 +186,19 @@ extern "C" int fp_autotune(fp_handle h, int* tile, int* tma_off, int* x_bulk, do
     if (tile) *tile = r.tile;
     if (tma_off) *tma_off = r.tma_off ? 1 : 0;
     if (x_bulk) *x_bulk = r.x_bulk ? 1 : 0;
+    if (x_rows) *x_rows = r.x_rows;
     if (apply_ms) *apply_ms = r.ms;
     return FP_OK;
 }
 
-extern "C" int fp_set_tiling(fp_handle h, int tile, int tma_off, int x_bulk) {
+extern "C" int fp_set_tiling(fp_handle h, int tile, int tma_off, int x_bulk, int x_rows) {
     using namespace fp;
     if (!h) return FP_ERR_INVALID;
     if (tile != 0 && tile != 2 && tile != 4 && tile != 8 && tile != 16 && tile != 32) {
         h->P.err = "fp_set_tiling: tile must be 0 (default), 2, 4, 8, 16 or 32";
         return FP_ERR_INVALID;
     }
-    apply_tiling(h->P, tile, tma_off != 0, x_bulk != 0);
+    apply_tiling(h->P, tile, tma_off != 0, x_bulk != 0, x_rows < 0 ? 0 : x_rows);
     return FP_OK;
 }
 

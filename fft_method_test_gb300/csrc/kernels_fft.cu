@@ -211,6 +211,8 @@ static int choose_rows_per_cta(const Problem& P, int tpl, int ld, size_t elem) {
     if (rows > P.nrows) rows = (int)P.nrows;
     // enough CTAs to fill the machine
     while (rows > 2 && (P.nrows + rows - 1) / rows < 2LL * P.sm_count) rows -= 2;
+    // a tuned cap (fewer rows: smaller CTAs, more of them per SM)
+    if (P.x_rows > 0 && P.x_rows < rows) rows = P.x_rows;
     return rows;
 }
 
