@@ -60,7 +60,8 @@ def parse():
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--mode", default="solve", choices=["solve", "apply", "batch", "learned"],
+    ap.add_argument("--mode", default="solve",
+                    choices=["solve", "apply", "batch", "learned", "brinkman"],
                     help="apply: only run --reps operator applies per precision (for profilers)")
     ap.add_argument("--precision", default="mixed,fp64", help="precisions for --mode apply")
     ap.add_argument("--reps", type=int, default=3)
@@ -561,8 +562,72 @@ def run_learned(args):
     print(json.dumps(line), flush=True)
 
 
+def run_brinkman(args):
+    """C2: Brinkman penalisation on a 128^3 cell of radius-8 spheres at
+    porosity 0.45 (seed 1002), penalty 1e4, viscosity 1, unit force along x.
+    Times the reference iteration on the GPU (per-iteration HBM roofline:
+    1016 bytes per voxel), the fixed-point solver to tol 1e-8, and the
+    reference iteration on the CPU oracle (single thread, as the reference's
+    Brinkman builds) on a bounded sample."""
+    import torch
+
+    from fft_method_test_gb300 import geometry as G
+    from fft_method_test_gb300.permeability import solveBrinkman, solveBrinkmanFixedPoint
+
+    mask = G.spheres(128, 8.0, 0.45, seed=1002)
+    ids = G.to_ids(mask)
+    n = ids.size
+    its = 400  # the reference's default max_iterations
+    solveBrinkman(ids, (1.0, 0.0, 0.0), solid_penalty=1e4, tolerance=1e-30, max_iterations=10)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ref = solveBrinkman(ids, (1.0, 0.0, 0.0), solid_penalty=1e4, tolerance=1e-30, max_iterations=its)
+    t_ref = time.perf_counter() - t0
+    peak, peak_kind = measured_peak_hbm()
+    bytes_it = 1016.0 * n
+    achieved = bytes_it * its / t_ref / 1e9
+    solveBrinkmanFixedPoint(ids, (1.0, 0.0, 0.0), solid_penalty=1e4, tolerance=1e-6)
+    t0 = time.perf_counter()
+    fpnt = solveBrinkmanFixedPoint(ids, (1.0, 0.0, 0.0), solid_penalty=1e4, tolerance=1e-8)
+    t_fp = time.perf_counter() - t0
+    U_fp = fpnt["superficialVelocity"]
+    cpu = None
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as orc
+
+        R = orc.Restatement()
+        k = 5
+        t0 = time.perf_counter()
+        R.brinkman(ids, tolerance=1e-30, max_iterations=k)
+        t_cpu = (time.perf_counter() - t0) / k
+        cpu = {"value": t_cpu * its, "unit": "s", "cores": 1, "kind": "port",
+               "sample": "C restatement of the reference iteration, %d iterations at 128^3 "
+                         "timed (%.3f s each), scaled to %d" % (k, t_cpu, its)}
+    line = {"metric": "brinkman_c2_128", "data": "synthetic", "n_gpus": 1, "dtype": "fp64",
+            "config": {"workload": "spheres128_r8_phi0.45_seed1002", "penalty": 1e4, "mu": 1.0,
+                       "force": [1.0, 0.0, 0.0]},
+            "reference_iteration": {"iterations": its, "seconds": t_ref,
+                                    "ms_per_iteration": 1e3 * t_ref / its,
+                                    "residual": ref["residual"],
+                                    "U_rel_err_vs_fixed_point":
+                                        float(abs(ref["superficialVelocity"][0] - U_fp[0]) / abs(U_fp[0])),
+                                    "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                                                 "unit": "GB/s", "frac": achieved / peak,
+                                                 "peak_kind": peak_kind,
+                                                 "bytes_per_iteration": bytes_it}},
+            "fixed_point": {"tol": 1e-8, "iterations": fpnt["iterations"], "seconds": t_fp,
+                            "converged": bool(fpnt["converged"]), "residual": fpnt["residual"],
+                            "U": [float(u) for u in U_fp]},
+            "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.mode == "brinkman":
+        run_brinkman(args)
+        return
     if args.mode == "learned":
         run_learned(args)
         return
