@@ -166,9 +166,11 @@ __global__ void __launch_bounds__(256, 3) k_xfwd(XArgs a) {
                 const int x = (int)(idx - (r0 + rl) * nx);
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    double val = 0.0;
-                    if (SRC != kSrcF0) val = cv[u][c] - mean[c];
-                    if (SRC != kSrcCompact) val += a.f0_support[c];
+                    // in the FP32 apply the value is rounded to FP32 anyway:
+                    // form it in FP32 (GB300's FP64 pipe is narrow)
+                    T val = (T)0;
+                    if (SRC != kSrcF0) val = (T)cv[u][c] - (T)mean[c];
+                    if (SRC != kSrcCompact) val += (T)a.f0_support[c];
                     const int L = 3 * rl + c;
                     T2* p = &lines[(L >> 1) * ld + pidx<T2>(x)];
                     if (L & 1) p->y = (T)val; else p->x = (T)val;
@@ -625,7 +627,7 @@ __device__ __forceinline__ void xinv_tile(const XArgs& a, c_t<T>* lines, long lo
             for (int c = 0; c < 3; ++c) {
                 const int L = 3 * rl + c;
                 const T2 zv = lines[(L >> 1) * ld + pidx<T2>(x)];
-                const double val = (double)((L & 1) ? zv.y : zv.x) * a.scale;
+                const double val = (double)(((L & 1) ? zv.y : zv.x) * (T)a.scale);
                 a.dst[3LL * s + c] = val;
                 acc[c] += val;
                 if (a.dot_with) acc[3] += a.dot_with[3LL * s + c] * val;
@@ -639,7 +641,7 @@ __device__ __forceinline__ void xinv_tile(const XArgs& a, c_t<T>* lines, long lo
             const int rl = L / 3;
             const int c = L - 3 * rl;
             const T2 zv = lines[(L >> 1) * ld + pidx<T2>(x)];
-            const double val = (double)((L & 1) ? zv.y : zv.x) * a.scale;
+            const double val = (double)(((L & 1) ? zv.y : zv.x) * (T)a.scale);
             a.dst[c * a.n + (r0 + rl) * nx + x] = val;
             acc[c] += val;
         }

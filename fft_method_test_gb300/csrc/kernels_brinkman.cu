@@ -41,16 +41,23 @@ struct BrState {
 struct BrGrid {
     int nx, ny, nz;
     long long n;
+    int nrows;  // ny * nz
 };
 
-__device__ __forceinline__ void nbrs(const BrGrid& g, long long id, long long& xm, long long& xp,
-                                     long long& ym, long long& yp, long long& zm, long long& zp) {
-    const int x = (int)(id % g.nx);
-    const long long r = id / g.nx;
-    const int y = (int)(r % g.ny);
-    const int z = (int)(r / g.ny);
+// Voxel loop of the stencil kernels: CTAs stride over the ny*nz grid rows,
+// threads over x, so neighbour indices need no per-voxel integer division.
+#define BR_FOR_VOXELS(g, row, x)                                      \
+    for (int row = blockIdx.x; row < (g).nrows; row += gridDim.x)     \
+        for (int x = threadIdx.x; x < (g).nx; x += blockDim.x)
+
+__device__ __forceinline__ void nbrs(const BrGrid& g, int row, int x, long long& id, long long& xm,
+                                     long long& xp, long long& ym, long long& yp, long long& zm,
+                                     long long& zp) {
+    const int y = row % g.ny;
+    const int z = row / g.ny;
     const long long sxy = (long long)g.nx * g.ny;
-    const long long base = id - x;
+    const long long base = (long long)row * g.nx;
+    id = base + x;
     xm = base + (x == 0 ? g.nx - 1 : x - 1);
     xp = base + (x == g.nx - 1 ? 0 : x + 1);
     const long long rowz = (long long)z * sxy + x;
@@ -69,10 +76,9 @@ __global__ void k_br_momentum(BrGrid g, const BrState* st, const uint8_t* __rest
                               double* __restrict__ sx, double* __restrict__ sy,
                               double* __restrict__ sz) {
     if (st->done) return;
-    for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < g.n;
-         id += (long long)gridDim.x * blockDim.x) {
-        long long xm, xp, ym, yp, zm, zp;
-        nbrs(g, id, xm, xp, ym, yp, zm, zp);
+    BR_FOR_VOXELS(g, row, x) {
+        long long id, xm, xp, ym, yp, zm, zp;
+        nbrs(g, row, x, id, xm, xp, ym, yp, zm, zp);
         const bool fl = fluid[id] != 0;
         const double mu = fl ? fluid_mu : 1.0;
         const double alpha = fl ? 0.0 : penalty;
@@ -99,10 +105,9 @@ __global__ void k_br_divergence(BrGrid g, const BrState* st, const double* __res
     if (st->done) return;
     __shared__ double red[32];
     double acc[1] = {0.0};
-    for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < g.n;
-         id += (long long)gridDim.x * blockDim.x) {
-        long long xm, xp, ym, yp, zm, zp;
-        nbrs(g, id, xm, xp, ym, yp, zm, zp);
+    BR_FOR_VOXELS(g, row, x) {
+        long long id, xm, xp, ym, yp, zm, zp;
+        nbrs(g, row, x, id, xm, xp, ym, yp, zm, zp);
         const double d = 0.5 * (sx[xp] - sx[xm]) + 0.5 * (sy[yp] - sy[ym]) + 0.5 * (sz[zp] - sz[zm]);
         div[id] = d;
         acc[0] += d * d;
@@ -125,10 +130,9 @@ __global__ void k_br_jacobi0(BrGrid g, const BrState* st, const double* __restri
 __global__ void k_br_jacobi(BrGrid g, const BrState* st, const double* __restrict__ phi,
                             const double* __restrict__ div, double* __restrict__ phin) {
     if (st->done) return;
-    for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < g.n;
-         id += (long long)gridDim.x * blockDim.x) {
-        long long xm, xp, ym, yp, zm, zp;
-        nbrs(g, id, xm, xp, ym, yp, zm, zp);
+    BR_FOR_VOXELS(g, row, x) {
+        long long id, xm, xp, ym, yp, zm, zp;
+        nbrs(g, row, x, id, xm, xp, ym, yp, zm, zp);
         const double nb = phi[xm] + phi[xp] + phi[ym] + phi[yp] + phi[zm] + phi[zp];
         phin[id] = (nb - div[id]) / 6.0;
     }
@@ -141,10 +145,9 @@ __global__ void k_br_project(BrGrid g, const BrState* st, const double* __restri
                              double* __restrict__ uy, double* __restrict__ uz,
                              double* __restrict__ p) {
     if (st->done) return;
-    for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < g.n;
-         id += (long long)gridDim.x * blockDim.x) {
-        long long xm, xp, ym, yp, zm, zp;
-        nbrs(g, id, xm, xp, ym, yp, zm, zp);
+    BR_FOR_VOXELS(g, row, x) {
+        long long id, xm, xp, ym, yp, zm, zp;
+        nbrs(g, row, x, id, xm, xp, ym, yp, zm, zp);
         const double gx = 0.5 * (phi[xp] - phi[xm]);
         const double gy = 0.5 * (phi[yp] - phi[ym]);
         const double gz = 0.5 * (phi[zp] - phi[zm]);
@@ -286,11 +289,15 @@ extern "C" int fp_brinkman_solve(int nx, int ny, int nz, const uint32_t* ids, ui
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int threads = 256;
-    long long blocks_ll = (n + threads - 1) / threads;
-    if (blocks_ll > 8LL * sms) blocks_ll = 8LL * sms;
-    const int blocks = (int)blocks_ll;
-    const BrGrid g{nx, ny, nz, n};
+    // one CTA walks whole grid rows (threads over x); the flat kernels use
+    // the same shape as a grid-stride loop
+    int threads = ((nx + 31) / 32) * 32;
+    if (threads > 256) threads = 256;
+    if (threads < 64) threads = 64;
+    const int nrows = ny * nz;
+    int blocks = nrows < 16 * sms ? nrows : 16 * sms;
+    if (blocks > 4096) blocks = 4096;  // partial-sum slots
+    const BrGrid g{nx, ny, nz, n, nrows};
 
     // one outer iteration, captured once and replayed
     cudaGraph_t graph = nullptr;

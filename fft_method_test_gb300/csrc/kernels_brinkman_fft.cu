@@ -82,13 +82,13 @@ __global__ void __launch_bounds__(kBfThreads) k_bf_stencil(BfGrid g, const BfSca
     double acc[4] = {0, 0, 0, 0};
     const long long n = g.n;
     const long long sxy = (long long)g.nx * g.ny;
-    for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < n;
-         id += (long long)gridDim.x * blockDim.x) {
-        const int x = (int)(id % g.nx);
-        const long long r = id / g.nx;
-        const int y = (int)(r % g.ny);
-        const int z = (int)(r / g.ny);
-        const long long base = id - x;
+    // CTAs stride over grid rows, threads over x: no per-voxel division
+    for (int row = blockIdx.x; row < g.ny * g.nz; row += gridDim.x)
+        for (int x = threadIdx.x; x < g.nx; x += blockDim.x) {
+        const int y = row % g.ny;
+        const int z = row / g.ny;
+        const long long base = (long long)row * g.nx;
+        const long long id = base + x;
         const long long xm = base + (x == 0 ? g.nx - 1 : x - 1);
         const long long xp = base + (x == g.nx - 1 ? 0 : x + 1);
         const long long rowz = (long long)z * sxy + x;
@@ -161,15 +161,12 @@ __global__ void __launch_bounds__(kBfThreads) k_bf_spectral(BfSpecArgs a, const 
     if (sc->done) return;
     const double g = MODE == 0 ? sc->g : 0.0;
     double acc[4] = {0, 0, 0, 0};
-    const long long tot = a.nrows * a.nxh;
     const bool even = (a.nx & 1) == 0;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot;
-         t += (long long)gridDim.x * blockDim.x) {
-        const long long row = t / a.nxh;
-        const int kx = (int)(t - row * a.nxh);
-        const int ky = (int)(row % a.ny);
-        const int kz = (int)(row / a.ny);
-        const long long i = row * a.rs + kx;
+    for (int row = blockIdx.x; row < (int)a.nrows; row += gridDim.x)
+        for (int kx = threadIdx.x; kx < a.nxh; kx += blockDim.x) {
+        const int ky = row % a.ny;
+        const int kz = row / a.ny;
+        const long long i = (long long)row * a.rs + kx;
         const double s0 = a.sx[kx], s1 = a.sy[ky], s2 = a.sz[kz];
         const double ss = s0 * s0 + s1 * s1 + s2 * s2;
         double2 v0 = a.spec[i], v1 = a.spec[a.nh + i], v2 = a.spec[2 * a.nh + i];
@@ -285,14 +282,11 @@ __global__ void k_bf_end(BfScalars* sc) {
 // p^ = -i s . (F(f) - a^) / |s|^2 into component 0 of spec, components 1, 2
 // zeroed (pressure gauge: zero on the s = 0 modes).
 __global__ void k_bf_pressure(BfSpecArgs a) {
-    const long long tot = a.nrows * a.nxh;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot;
-         t += (long long)gridDim.x * blockDim.x) {
-        const long long row = t / a.nxh;
-        const int kx = (int)(t - row * a.nxh);
-        const int ky = (int)(row % a.ny);
-        const int kz = (int)(row / a.ny);
-        const long long i = row * a.rs + kx;
+    for (int row = blockIdx.x; row < (int)a.nrows; row += gridDim.x)
+        for (int kx = threadIdx.x; kx < a.nxh; kx += blockDim.x) {
+        const int ky = row % a.ny;
+        const int kz = row / a.ny;
+        const long long i = (long long)row * a.rs + kx;
         const double s0 = a.sx[kx], s1 = a.sy[ky], s2 = a.sz[kz];
         const double ss = s0 * s0 + s1 * s1 + s2 * s2;
         const bool k0 = (row == 0 && kx == 0);
@@ -352,6 +346,8 @@ struct BfSolver {
     BfScalars* sc = nullptr;
     BfScalars* hsc = nullptr;
     int blocks = 0;
+    int tx = kBfThreads;  // threads of the x-walking kernels (grid rows)
+    int tk = kBfThreads;  // threads of the kx-walking kernels (spectral rows)
     ~BfSolver() {
         DeviceMemGuard mem_guard;
         cudaFree(x);
@@ -407,9 +403,17 @@ int bf_init(BfSolver& S, int nx, int ny, int nz, const uint8_t* fl_host) {
             "copy");
     BF_CUDA(cudaMemcpyAsync(S.fluid, fl_host, (size_t)P.n, cudaMemcpyHostToDevice, P.stream), "copy");
     BF_CUDA(cudaStreamSynchronize(P.stream), "sync");
-    long long b = (P.n + kBfThreads - 1) / kBfThreads;
-    if (b > 8LL * P.sm_count) b = 8LL * P.sm_count;
+    // row-walking kernels: up to 16 CTAs per SM, at most one per grid row,
+    // threads rounded up from the row length
+    long long b = P.nrows;
+    if (b > 16LL * P.sm_count) b = 16LL * P.sm_count;
     S.blocks = (int)b;
+    auto fit = [](long long len) {
+        long long t = (len + 31) / 32 * 32;
+        return (int)(t < 64 ? 64 : (t > kBfThreads ? kBfThreads : t));
+    };
+    S.tx = fit(P.nx);
+    S.tk = fit(P.nxh);
     return FP_OK;
 }
 
@@ -465,14 +469,14 @@ cudaError_t bf_iteration(BfSolver& S, const BfSpecArgs& sa, const BfGrid& g, dou
     Problem& P = S.h->P;
     const int* skip = &S.sc->done;
     FP_LAUNCHED();
-    k_bf_stencil<<<S.blocks, kBfThreads, 0, P.stream>>>(g, S.sc, S.fluid, penalty, S.p, S.w,
+    k_bf_stencil<<<S.blocks, S.tx, 0, P.stream>>>(g, S.sc, S.fluid, penalty, S.p, S.w,
                                                          P.d_partials);
     FP_LAUNCHED();
     k_bf_after_stencil<<<1, 256, 0, P.stream>>>(S.sc, P.d_partials, S.blocks);
     cudaError_t e = fft_forward_dense(P, S.w, skip);
     if (e != cudaSuccess) return e;
     FP_LAUNCHED();
-    k_bf_spectral<0><<<S.blocks, kBfThreads, 0, P.stream>>>(sa, S.sc);
+    k_bf_spectral<0><<<S.blocks, S.tk, 0, P.stream>>>(sa, S.sc);
     FP_LAUNCHED();
     k_bf_after_spectral<<<1, 256, 0, P.stream>>>(S.sc, P.d_partials, S.blocks, 1.0 / (double)P.n, 0);
     e = fft_inverse_dense(P, S.w, skip);
@@ -489,12 +493,12 @@ cudaError_t bf_iteration(BfSolver& S, const BfSpecArgs& sa, const BfGrid& g, dou
 cudaError_t bf_restart(BfSolver& S, const BfSpecArgs& sa, const BfGrid& g, double penalty) {
     Problem& P = S.h->P;
     FP_LAUNCHED();
-    k_bf_stencil<<<S.blocks, kBfThreads, 0, P.stream>>>(g, S.sc, S.fluid, penalty, S.x, S.w,
+    k_bf_stencil<<<S.blocks, S.tx, 0, P.stream>>>(g, S.sc, S.fluid, penalty, S.x, S.w,
                                                          P.d_partials);
     cudaError_t e = fft_forward_dense(P, S.w, nullptr);
     if (e != cudaSuccess) return e;
     FP_LAUNCHED();
-    k_bf_spectral<1><<<S.blocks, kBfThreads, 0, P.stream>>>(sa, S.sc);
+    k_bf_spectral<1><<<S.blocks, S.tk, 0, P.stream>>>(sa, S.sc);
     FP_LAUNCHED();
     k_bf_after_spectral<<<1, 256, 0, P.stream>>>(S.sc, P.d_partials, S.blocks, 1.0 / (double)P.n, 1);
     e = fft_inverse_dense(P, S.w, nullptr);
@@ -596,11 +600,11 @@ int bf_solve(BfSolver& S, double penalty, double tol, long long maxit, const dou
         rc = bf_write(S);
         if (rc) return rc;
         FP_LAUNCHED();
-        k_bf_stencil<<<S.blocks, kBfThreads, 0, P.stream>>>(g, S.sc, S.fluid, penalty, S.x, S.w,
+        k_bf_stencil<<<S.blocks, S.tx, 0, P.stream>>>(g, S.sc, S.fluid, penalty, S.x, S.w,
                                                              P.d_partials);
         BF_CUDA(fft_forward_dense(P, S.w, nullptr), "pressure FFT");
         FP_LAUNCHED();
-        k_bf_pressure<<<S.blocks, kBfThreads, 0, P.stream>>>(sa);
+        k_bf_pressure<<<S.blocks, S.tk, 0, P.stream>>>(sa);
         BF_CUDA(fft_inverse_dense(P, S.w, nullptr), "pressure FFT");
         BF_CUDA(cudaMemcpyAsync(p_out, S.w, sizeof(double) * P.n, cudaMemcpyDeviceToHost, P.stream),
                 "copy");
