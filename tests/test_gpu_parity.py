@@ -367,3 +367,21 @@ def test_largest_grid_512_apply_properties(gpu_lib):
         p.set_precision("mixed")
         Aa32 = p.operator_apply(a)
     assert rel_err(Aa32, Aa) < 5e-6
+
+
+@pytest.mark.parametrize("p_radius,h,mu,support", [(0, 1.0, 1.0, "interface"),
+                                                   (1, 0.5, 2.0, "interface"),
+                                                   (3, 1.0, 1.0, "interface"),
+                                                   (2, 1.0, 1.0, "fullsolid")])
+def test_permeability_variants_match_oracle(gpu_lib, restatement, p_radius, h, mu, support):
+    """The reference's other choices (alias radius p_radius of the Green sum,
+    voxel size, viscosity, FullSolid support): K within 1e-10 of the oracle."""
+    mask = G.spheres((12, 14, 16), 2.5, 0.6, seed=21)
+    mode = 0 if support == "interface" else 1
+    K_ref, _ = restatement.context(mask, h=h, mu=mu, p_radius=p_radius,
+                                   mode=mode).solve_permeability(1e-11, 4000)
+    with problem(mask.shape, voxel_size=h, mu=mu, p_radius=p_radius) as p:
+        p.set_geometry(mask, support)
+        K, st = p.solve_permeability(1e-11, 4000)
+    assert all(s["converged"] for s in st)
+    assert rel_err(K, K_ref) < 1e-9, rel_err(K, K_ref)
