@@ -63,6 +63,21 @@ __host__ __device__ __forceinline__ int line_stride(int n, int padsh) {
     return l | 1;
 }
 
+// Line stride for the passes whose threads run over columns first (y, z:
+// thread = column + t * position).  One shared-memory wavefront of 8-byte
+// (16-byte) accesses serves B = 16 (8) threads: min(t, B) columns times B/t
+// neighbouring positions of each line.  An odd stride separates the columns
+// when t >= B; for t < B a stride congruent to B/t modulo B puts the B/t
+// positions of every column in banks of their own.
+__host__ __device__ __forceinline__ int column_line_stride(int n, int padsh, int t, int elem) {
+    int ld = line_stride(n, padsh);
+    const int B = 128 / elem;
+    if (t >= B) return ld;
+    const int target = (B / t) % B;
+    while (ld % B != target) ++ld;
+    return ld;
+}
+
 template <typename T2>
 __device__ __forceinline__ const T2* plan_tw(const FftPlanDev& p);
 template <>

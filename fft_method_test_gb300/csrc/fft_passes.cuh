@@ -81,6 +81,7 @@ struct TmaTile {
     int np;        // component stride of the raw tile in rows: >= nbox * box, padded so
                    // that every component block starts 128-byte aligned
     int bufbytes;  // bytes of one tile buffer (raw tile or padded lines, larger of the two)
+    int ld;        // line stride of the padded lines (column_line_stride for t)
 };
 
 // ---------------------------------------------------------------------------

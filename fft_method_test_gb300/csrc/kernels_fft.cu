@@ -146,7 +146,7 @@ constexpr int kTmaSmemLimit = 227 * 1024;
 
 // Chooses the tiling of the TMA-fed y (axis 0) or z (axis 1) pass and builds
 // or reuses its descriptor.  Returns false when the TMA path does not apply.
-static bool tma_setup(Problem& P, bool dbl, int axis, int tpl, int ld, TmaTile& tt,
+static bool tma_setup(Problem& P, bool dbl, int axis, int tpl, int padsh, TmaTile& tt,
                       const CUtensorMap** map) {
     if (P.tma_off || !tma_encoder()) return false;
     const size_t e = dbl ? sizeof(double) : sizeof(float);
@@ -169,6 +169,8 @@ static bool tma_setup(Problem& P, bool dbl, int axis, int tpl, int ld, TmaTile& 
         tt.np = tt.nbox * tt.box;
         while (((size_t)tt.np * t * e2) % 128 != 0) ++tt.np;
         const size_t raw = (size_t)3 * tt.np * t * e2;
+        const int ld = column_line_stride(n, padsh, t, (int)e2);
+        tt.ld = ld;
         const size_t lines = (size_t)3 * t * ld * e2;
         const size_t buf = ((raw > lines ? raw : lines) + 127) & ~size_t(127);
         if (128 + 2 * buf > (size_t)kTmaSmemLimit) continue;
@@ -274,12 +276,14 @@ static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     y.skip = aa.skip;
     y.err = P.d_err;
     y.nz = P.nz;
-    y.ld = line_stride(P.ny, padsh);
+    const int bank_row = 128 / (int)elem;  // elements per shared-memory bank row
     const int tply = tpl_of(P.py);
     {
+        const int ld_max = line_stride(P.ny, padsh) + bank_row;
         int tx = P.tile_yz > 0 ? P.tile_yz : (dbl ? 8 : 16);
-        while (tx > 1 && (tx * tply > max_yz || (size_t)3 * tx * y.ld * elem > 110 * 1024)) tx /= 2;
+        while (tx > 1 && (tx * tply > max_yz || (size_t)3 * tx * ld_max * elem > 110 * 1024)) tx /= 2;
         y.tx = tx;
+        y.ld = column_line_stride(P.ny, padsh, tx, (int)elem);
     }
     const int ythreads = y.tx * tply;
     const size_t ysmem = (size_t)3 * y.tx * y.ld * elem;
@@ -299,12 +303,13 @@ static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     z.spec = P.d_spec;
     z.skip = aa.skip;
     z.err = P.d_err;
-    z.ld = line_stride(P.nz, padsh);
     const int tplz = tpl_of(P.pz);
     {
+        const int ld_max = line_stride(P.nz, padsh) + bank_row;
         int tz = P.tile_yz > 0 ? P.tile_yz : (dbl ? 8 : 16);
-        while (tz > 1 && (tz * tplz > max_yz || (size_t)3 * tz * z.ld * elem > 110 * 1024)) tz /= 2;
+        while (tz > 1 && (tz * tplz > max_yz || (size_t)3 * tz * ld_max * elem > 110 * 1024)) tz /= 2;
         z.tz = tz;
+        z.ld = column_line_stride(P.nz, padsh, tz, (int)elem);
     }
     const int zthreads = z.tz * tplz;
     const size_t zsmem = (size_t)3 * z.tz * z.ld * elem;
@@ -313,14 +318,25 @@ static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     TmaTile tty{}, ttz{};
     const CUtensorMap* mapy = nullptr;
     const CUtensorMap* mapz = nullptr;
-    const bool tma_y = P.d_err && tma_setup(P, dbl, 0, tply, y.ld, tty, &mapy);
-    const bool tma_z = P.d_err && tma_setup(P, dbl, 1, tplz, z.ld, ttz, &mapz);
+    const bool tma_y = P.d_err && tma_setup(P, dbl, 0, tply, padsh, tty, &mapy);
+    const bool tma_z = P.d_err && tma_setup(P, dbl, 1, tplz, padsh, ttz, &mapz);
     const int ygrid_tma = (int)std::min<long long>(tty.ntiles, P.sm_count);
     const int zgrid_tma = (int)std::min<long long>(ttz.ntiles, P.sm_count);
     const size_t ysmem_tma = 128 + 2 * (size_t)tty.bufbytes;
     const size_t zsmem_tma = 128 + 2 * (size_t)ttz.bufbytes;
-    if (tma_y) y.tx = tty.t;
-    if (tma_z) z.tz = ttz.t;
+    // the TMA-fed passes get their own tile width and line stride; the
+    // register-fed kernels (also the forward-only / inverse-only z passes)
+    // keep the ones their launch shape was computed from
+    YArgs yt = y;
+    ZArgs zt = z;
+    if (tma_y) {
+        yt.tx = tty.t;
+        yt.ld = tty.ld;
+    }
+    if (tma_z) {
+        zt.tz = ttz.t;
+        zt.ld = ttz.ld;
+    }
 
     cudaStream_t st = P.stream;
     cudaError_t e = cudaSuccess;
@@ -332,7 +348,7 @@ static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     if (aa.stage != kStageInverse) {
         FP_CHECK(run_xfwd<T>(aa.src_kind, x, xblocks, xthreads, xsmem, st));
         if (tma_y)
-            FP_CHECK(run_ypass_tma<T>(-1, *mapy, y, tty, ygrid_tma, tty.t * tply, ysmem_tma, st));
+            FP_CHECK(run_ypass_tma<T>(-1, *mapy, yt, tty, ygrid_tma, tty.t * tply, ysmem_tma, st));
         else if (P.ny > 1)
             FP_CHECK(run_ypass<T>(-1, y, ygrid, ythreads, ysmem, st));
         if (aa.stage == kStageForward) {
@@ -340,14 +356,14 @@ static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
             return cudaSuccess;
         }
         if (tma_z)
-            FP_CHECK(run_zgreen_tma<T>(*mapz, z, ttz, zgrid_tma, ttz.t * tplz, zsmem_tma, st));
+            FP_CHECK(run_zgreen_tma<T>(*mapz, zt, ttz, zgrid_tma, ttz.t * tplz, zsmem_tma, st));
         else
             FP_CHECK(run_zgreen<T>(0, z, zgrid, zthreads, zsmem, st));
     } else {
         FP_CHECK(run_zgreen<T>(2, z, zgrid, zthreads, zsmem, st));
     }
     if (tma_y)
-        FP_CHECK(run_ypass_tma<T>(+1, *mapy, y, tty, ygrid_tma, tty.t * tply, ysmem_tma, st));
+        FP_CHECK(run_ypass_tma<T>(+1, *mapy, yt, tty, ygrid_tma, tty.t * tply, ysmem_tma, st));
     else if (P.ny > 1)
         FP_CHECK(run_ypass<T>(+1, y, ygrid, ythreads, ysmem, st));
     // inverse x: persistent bulk-copy pipeline when it fits, else one tile per CTA
