@@ -66,7 +66,8 @@ def parse():
     ap.add_argument("--precision", default="mixed,fp64", help="precisions for --mode apply")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--tiling", default="",
-                    help="--mode apply: 'auto' (autotune) or 'tile,tma,x_bulk,x_rows' (e.g. 8,0,1,0)")
+                    help="--mode apply: 'auto' (autotune) or 'tile,tma,x_bulk,x_rows[,lowreg]' "
+                         "(e.g. 8,0,1,0)")
     ap.add_argument("--batch-count", type=int, default=64, help="microstructures for --mode batch")
     ap.add_argument("--concurrency", type=int, default=8, help="host threads for --mode batch")
     return ap.parse_args()
@@ -450,8 +451,8 @@ def run_applies(args):
             if args.tiling == "auto":
                 print(prec, "tiling", p.autotune(), flush=True)
             elif args.tiling:
-                t, tma, xb, xr = (int(v) for v in args.tiling.split(","))
-                p.set_tiling(t, bool(tma), bool(xb), xr)
+                t, tma, xb, xr, lo = (int(v) for v in (args.tiling + ",0").split(",")[:5])
+                p.set_tiling(t, bool(tma), bool(xb), xr, bool(lo))
             x = torch.randn(3 * nb, dtype=torch.float64, device="cuda")
             y = torch.empty_like(x)
             torch.cuda.synchronize()

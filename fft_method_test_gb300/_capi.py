@@ -111,8 +111,9 @@ _SIGNATURES = {
                                   C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
                                   C.c_double, _dp, C.POINTER(BrinkmanStats)], C.c_int),
     "fp_brinkman_last_error": ([], C.c_char_p),
-    "fp_autotune": ([_h, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
-    "fp_set_tiling": ([_h, C.c_int, C.c_int, C.c_int, C.c_int], C.c_int),
+    "fp_autotune": ([_h, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
+                    C.c_int),
+    "fp_set_tiling": ([_h, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int], C.c_int),
     "fp_batch_solve_permeability": ([C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
                                      C.c_int, C.c_int, C.c_int, C.c_double, C.c_int64, C.c_int,
                                      C.c_int, _dp, C.c_void_p, C.c_void_p], C.c_int),

@@ -50,6 +50,7 @@ struct TuneResult {
     bool tma_off = false;
     bool x_bulk = true;
     int x_rows = 0;
+    bool yz_lowreg = false;
     double ms = 0.0;
 };
 
@@ -58,9 +59,12 @@ std::map<TuneKey, TuneResult> g_tune_cache;
 
 thread_local std::string g_batch_error;
 
-void apply_tiling(Problem& P, int tile, bool tma_off, bool x_bulk, int x_rows) {
-    if (P.tile_yz == tile && P.tma_off == tma_off && P.x_bulk == x_bulk && P.x_rows == x_rows) return;
+void apply_tiling(Problem& P, int tile, bool tma_off, bool x_bulk, int x_rows, bool lowreg) {
+    if (P.tile_yz == tile && P.tma_off == tma_off && P.x_bulk == x_bulk && P.x_rows == x_rows &&
+        P.yz_lowreg == lowreg)
+        return;
     release_graphs(P);
+    P.yz_lowreg = lowreg;
     P.tile_yz = tile;
     P.tma_off = tma_off;
     P.x_bulk = x_bulk;
@@ -122,7 +126,7 @@ int tune(Problem& P, TuneResult* out) {
         auto it = g_tune_cache.find(key);
         if (it != g_tune_cache.end()) {
             *out = it->second;
-            apply_tiling(P, out->tile, out->tma_off, out->x_bulk, out->x_rows);
+            apply_tiling(P, out->tile, out->tma_off, out->x_bulk, out->x_rows, out->yz_lowreg);
             return FP_OK;
         }
     }
@@ -130,33 +134,39 @@ int tune(Problem& P, TuneResult* out) {
     const bool tma0 = P.tma_off;
     const bool bulk0 = P.x_bulk;
     const int rows0 = P.x_rows;
+    const bool low0 = P.yz_lowreg;
     TuneResult best;
     best.ms = 1e30;
     const int tiles[] = {4, 8, 16, 32};
     const int xrows[] = {0, 4, 2};
+    // the register-capped y/z kernels exist for the FP32 register-fed passes
+    const int nlow = P.precision == kFP64 ? 1 : 2;
     for (int xr : xrows) {
         for (int xb = 0; xb < 2; ++xb) {
             for (int off = 0; off < 2; ++off) {
-                for (int t : tiles) {
-                    apply_tiling(P, t, off != 0, xb == 0, xr);
-                    double ms = 0.0;
-                    const int rc = time_apply(P, 3, &ms);
-                    if (rc != FP_OK) {
-                        apply_tiling(P, tile0, tma0, bulk0, rows0);
-                        return rc;
-                    }
-                    if (ms < best.ms) {
-                        best.ms = ms;
-                        best.tile = t;
-                        best.tma_off = off != 0;
-                        best.x_bulk = xb == 0;
-                        best.x_rows = xr;
+                for (int lo = 0; lo < (off ? nlow : 1); ++lo) {
+                    for (int t : tiles) {
+                        apply_tiling(P, t, off != 0, xb == 0, xr, lo != 0);
+                        double ms = 0.0;
+                        const int rc = time_apply(P, 3, &ms);
+                        if (rc != FP_OK) {
+                            apply_tiling(P, tile0, tma0, bulk0, rows0, low0);
+                            return rc;
+                        }
+                        if (ms < best.ms) {
+                            best.ms = ms;
+                            best.tile = t;
+                            best.tma_off = off != 0;
+                            best.x_bulk = xb == 0;
+                            best.x_rows = xr;
+                            best.yz_lowreg = lo != 0;
+                        }
                     }
                 }
             }
         }
     }
-    apply_tiling(P, best.tile, best.tma_off, best.x_bulk, best.x_rows);
+    apply_tiling(P, best.tile, best.tma_off, best.x_bulk, best.x_rows, best.yz_lowreg);
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         g_tune_cache[key] = best;
@@ -174,7 +184,7 @@ struct Job {
 }  // namespace fp
 
 extern "C" int fp_autotune(fp_handle h, int* tile, int* tma_off, int* x_bulk, int* x_rows,
-                           double* apply_ms) {
+                           int* lowreg, double* apply_ms) {
     using namespace fp;
     if (!h) return FP_ERR_INVALID;
     TuneResult r;
@@ -187,18 +197,19 @@ extern "C" int fp_autotune(fp_handle h, int* tile, int* tma_off, int* x_bulk, in
     if (tma_off) *tma_off = r.tma_off ? 1 : 0;
     if (x_bulk) *x_bulk = r.x_bulk ? 1 : 0;
     if (x_rows) *x_rows = r.x_rows;
+    if (lowreg) *lowreg = r.yz_lowreg ? 1 : 0;
     if (apply_ms) *apply_ms = r.ms;
     return FP_OK;
 }
 
-extern "C" int fp_set_tiling(fp_handle h, int tile, int tma_off, int x_bulk, int x_rows) {
+extern "C" int fp_set_tiling(fp_handle h, int tile, int tma_off, int x_bulk, int x_rows, int lowreg) {
     using namespace fp;
     if (!h) return FP_ERR_INVALID;
     if (tile != 0 && tile != 2 && tile != 4 && tile != 8 && tile != 16 && tile != 32) {
         h->P.err = "fp_set_tiling: tile must be 0 (default), 2, 4, 8, 16 or 32";
         return FP_ERR_INVALID;
     }
-    apply_tiling(h->P, tile, tma_off != 0, x_bulk != 0, x_rows < 0 ? 0 : x_rows);
+    apply_tiling(h->P, tile, tma_off != 0, x_bulk != 0, x_rows < 0 ? 0 : x_rows, lowreg != 0);
     return FP_OK;
 }
 

@@ -236,7 +236,7 @@ struct ColIo {
 };
 
 template <typename T, int S>
-__global__ void __launch_bounds__(256) k_ypass(YArgs a) {
+__device__ __forceinline__ void ypass_body(const YArgs& a) {
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -255,6 +255,19 @@ __global__ void __launch_bounds__(256) k_ypass(YArgs a) {
 #pragma unroll
     for (int l = 0; l < 3; ++l) sl[l] = lines + (l * tx + c) * a.ld;
     fft_lines<S, kIoFunc, kIoFunc, 3>(sl, a.plan, lane, active, S > 0, io, io);
+}
+
+template <typename T, int S>
+__global__ void __launch_bounds__(256) k_ypass(YArgs a) {
+    ypass_body<T, S>(a);
+}
+
+// The same pass capped at 168 registers: 12 instead of 8 warps of 128-thread
+// CTAs per SM, at the price of a few hundred bytes of spills per thread.
+// The autotuner chooses between the two.
+template <typename T, int S>
+__global__ void __maxnreg__(168) k_ypass_lr(YArgs a) {
+    ypass_body<T, S>(a);
 }
 
 // ---------------------------------------------------------------------------
@@ -365,7 +378,7 @@ __device__ __forceinline__ void z_fused_rt(const ZArgs& a, c_t<T>* const* sl, Sr
 // ZMODE: 0 = forward z, Green multiply, inverse z; 1 = forward z only;
 // 2 = inverse z only
 template <typename T, int ZMODE>
-__global__ void __launch_bounds__(256) k_zgreen(ZArgs a) {
+__device__ __forceinline__ void zgreen_body(const ZArgs& a) {
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -404,6 +417,17 @@ __global__ void __launch_bounds__(256) k_zgreen(ZArgs a) {
         }
         z_fused_rt<T, kIoFunc>(a, sl, io, io, (long long)blockIdx.y * a.rs + k0 + c, lane, active);
     }
+}
+
+template <typename T, int ZMODE>
+__global__ void __launch_bounds__(256) k_zgreen(ZArgs a) {
+    zgreen_body<T, ZMODE>(a);
+}
+
+// capped at 168 registers (see k_ypass_lr)
+template <typename T, int ZMODE>
+__global__ void __maxnreg__(168) k_zgreen_lr(ZArgs a) {
+    zgreen_body<T, ZMODE>(a);
 }
 
 // ---------------------------------------------------------------------------
@@ -757,12 +781,14 @@ template <typename T>
 cudaError_t run_xinv_bulk(int dst_kind, const XArgs& x, int raw_bytes, int grid, int threads,
                           size_t smem, cudaStream_t s);
 template <typename T>
-cudaError_t run_ypass(int dir, const YArgs& y, dim3 grid, int threads, size_t smem, cudaStream_t s);
+cudaError_t run_ypass(int dir, const YArgs& y, dim3 grid, int threads, size_t smem, cudaStream_t s,
+                      bool lowreg);
 template <typename T>
 cudaError_t run_ypass_tma(int dir, const CUtensorMap& map, const YArgs& y, const TmaTile& tt, int grid,
                           int threads, size_t smem, cudaStream_t s);
 template <typename T>
-cudaError_t run_zgreen(int mode, const ZArgs& z, dim3 grid, int threads, size_t smem, cudaStream_t s);
+cudaError_t run_zgreen(int mode, const ZArgs& z, dim3 grid, int threads, size_t smem, cudaStream_t s,
+                       bool lowreg);
 template <typename T>
 cudaError_t run_zgreen_tma(const CUtensorMap& map, const ZArgs& z, const TmaTile& tt, int grid,
                            int threads, size_t smem, cudaStream_t s);
@@ -829,7 +855,17 @@ cudaError_t run_xinv_bulk(int dst_kind, const XArgs& x, int raw_bytes, int grid,
 
 #ifdef FP_DEFINE_Y_RUNNERS
 template <typename T>
-cudaError_t run_ypass(int dir, const YArgs& y, dim3 grid, int threads, size_t smem, cudaStream_t s) {
+cudaError_t run_ypass(int dir, const YArgs& y, dim3 grid, int threads, size_t smem, cudaStream_t s,
+                      bool lowreg) {
+    if constexpr (sizeof(T) == 4) {
+        if (lowreg) {
+            if (dir < 0)
+                FP_RUN((k_ypass_lr<T, -1>), grid, threads, smem, s, y);
+            else
+                FP_RUN((k_ypass_lr<T, +1>), grid, threads, smem, s, y);
+            return cudaGetLastError();
+        }
+    }
     if (dir < 0)
         FP_RUN((k_ypass<T, -1>), grid, threads, smem, s, y);
     else
@@ -849,7 +885,14 @@ cudaError_t run_ypass_tma(int dir, const CUtensorMap& map, const YArgs& y, const
 
 #ifdef FP_DEFINE_Z_RUNNERS
 template <typename T>
-cudaError_t run_zgreen(int mode, const ZArgs& z, dim3 grid, int threads, size_t smem, cudaStream_t s) {
+cudaError_t run_zgreen(int mode, const ZArgs& z, dim3 grid, int threads, size_t smem, cudaStream_t s,
+                       bool lowreg) {
+    if constexpr (sizeof(T) == 4) {
+        if (lowreg && mode == 0) {
+            FP_RUN((k_zgreen_lr<T, 0>), grid, threads, smem, s, z);
+            return cudaGetLastError();
+        }
+    }
     switch (mode) {
         case 0: FP_RUN((k_zgreen<T, 0>), grid, threads, smem, s, z); break;
         case 1: FP_RUN((k_zgreen<T, 1>), grid, threads, smem, s, z); break;

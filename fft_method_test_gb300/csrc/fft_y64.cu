@@ -4,7 +4,7 @@
 #include "fft_passes.cuh"
 
 namespace fp {
-template cudaError_t run_ypass<double>(int, const YArgs&, dim3, int, size_t, cudaStream_t);
+template cudaError_t run_ypass<double>(int, const YArgs&, dim3, int, size_t, cudaStream_t, bool);
 template cudaError_t run_ypass_tma<double>(int, const CUtensorMap&, const YArgs&, const TmaTile&, int, int,
                                       size_t, cudaStream_t);
 }  // namespace fp

@@ -5,5 +5,5 @@
 #include "fft_passes.cuh"
 
 namespace fp {
-template cudaError_t run_zgreen<float>(int, const ZArgs&, dim3, int, size_t, cudaStream_t);
+template cudaError_t run_zgreen<float>(int, const ZArgs&, dim3, int, size_t, cudaStream_t, bool);
 }  // namespace fp

@@ -142,6 +142,7 @@ struct Problem {
     bool tma_off = false;      // FFTPERM_NO_TMA=1 selects the register-fed passes
     bool x_bulk = true;        // inverse x pass fed by bulk copies (tuned)
     int x_rows = 0;            // cap on grid rows per CTA of the x passes (0 = none; tuned)
+    bool yz_lowreg = false;    // FP32 register-fed y/z passes capped at 168 registers (tuned)
     int* d_err = nullptr;      // device error flag (a bounded wait gave up)
 
     std::string err;

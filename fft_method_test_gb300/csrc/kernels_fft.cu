@@ -350,22 +350,22 @@ static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
         if (tma_y)
             FP_CHECK(run_ypass_tma<T>(-1, *mapy, yt, tty, ygrid_tma, tty.t * tply, ysmem_tma, st));
         else if (P.ny > 1)
-            FP_CHECK(run_ypass<T>(-1, y, ygrid, ythreads, ysmem, st));
+            FP_CHECK(run_ypass<T>(-1, y, ygrid, ythreads, ysmem, st, P.yz_lowreg));
         if (aa.stage == kStageForward) {
-            FP_CHECK(run_zgreen<T>(1, z, zgrid, zthreads, zsmem, st));
+            FP_CHECK(run_zgreen<T>(1, z, zgrid, zthreads, zsmem, st, P.yz_lowreg));
             return cudaSuccess;
         }
         if (tma_z)
             FP_CHECK(run_zgreen_tma<T>(*mapz, zt, ttz, zgrid_tma, ttz.t * tplz, zsmem_tma, st));
         else
-            FP_CHECK(run_zgreen<T>(0, z, zgrid, zthreads, zsmem, st));
+            FP_CHECK(run_zgreen<T>(0, z, zgrid, zthreads, zsmem, st, P.yz_lowreg));
     } else {
-        FP_CHECK(run_zgreen<T>(2, z, zgrid, zthreads, zsmem, st));
+        FP_CHECK(run_zgreen<T>(2, z, zgrid, zthreads, zsmem, st, P.yz_lowreg));
     }
     if (tma_y)
         FP_CHECK(run_ypass_tma<T>(+1, *mapy, yt, tty, ygrid_tma, tty.t * tply, ysmem_tma, st));
     else if (P.ny > 1)
-        FP_CHECK(run_ypass<T>(+1, y, ygrid, ythreads, ysmem, st));
+        FP_CHECK(run_ypass<T>(+1, y, ygrid, ythreads, ysmem, st, P.yz_lowreg));
     // inverse x: persistent bulk-copy pipeline when it fits, else one tile per CTA
     XArgs xb = x;
     int raw_bytes = 0;

@@ -101,17 +101,18 @@ class PermeabilityProblem:
 
     def autotune(self) -> dict:
         """fp_autotune: picks the fastest FFT tiling for this grid."""
-        tile, off, xb, xr = C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0)
+        tile, off, xb, xr, lo = C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0)
         ms = C.c_double(0.0)
         self._check(self.lib.fp_autotune(self._h, C.byref(tile), C.byref(off), C.byref(xb),
-                                         C.byref(xr), C.byref(ms)))
+                                         C.byref(xr), C.byref(lo), C.byref(ms)))
         return dict(tile=tile.value, tma=not off.value, x_bulk=bool(xb.value), x_rows=xr.value,
-                    apply_ms=ms.value)
+                    lowreg=bool(lo.value), apply_ms=ms.value)
 
-    def set_tiling(self, tile: int = 0, tma: bool = True, x_bulk: bool = True, x_rows: int = 0):
+    def set_tiling(self, tile: int = 0, tma: bool = True, x_bulk: bool = True, x_rows: int = 0,
+                   lowreg: bool = False):
         """fp_set_tiling: a given FFT tiling (e.g. one autotune reported)."""
         self._check(self.lib.fp_set_tiling(self._h, int(tile), int(not tma), int(x_bulk),
-                                           int(x_rows)))
+                                           int(x_rows), int(lowreg)))
 
     def set_geometry(self, fluid_mask: np.ndarray, support: str = "interface") -> int:
         m = np.ascontiguousarray(fluid_mask, dtype=np.uint8)

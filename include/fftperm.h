@@ -161,17 +161,20 @@ int fp_write_fvel(const char* path, int nx, int ny, int nz, double porosity, dou
 
 /* Times the operator apply of this handle for each y/z-pass tiling (kx
  * columns per CTA in {4, 8, 16, 32}, TMA-fed or register-fed) and each
- * inverse-x variant (bulk-copy pipelined or one tile per CTA) and x-pass
- * rows per CTA (no cap, 4, 2), and keeps the fastest; the choice is cached per (grid, precision) for the process and
+ * inverse-x variant (bulk-copy pipelined or one tile per CTA), x-pass
+ * rows per CTA (no cap, 4, 2) and, for FP32 register-fed y/z passes, a
+ * 168-register variant, and keeps the fastest; the choice is cached per (grid, precision) for the process and
  * applied to later fp_autotune calls on the same grid without timing.
  * Tiling changes the schedule and the grouping of partial sums (results equal
  * to rounding).  Outputs may be NULL. */
-int fp_autotune(fp_handle h, int* tile, int* tma_off, int* x_bulk, int* x_rows, double* apply_ms);
+int fp_autotune(fp_handle h, int* tile, int* tma_off, int* x_bulk, int* x_rows, int* lowreg,
+                double* apply_ms);
 /* Sets a tiling directly (for example one fp_autotune reported earlier):
  * tile in {0 = default, 2, 4, 8, 16, 32}, tma_off != 0 for the register-fed
  * y/z passes, x_bulk != 0 for the bulk-copy inverse x pass, x_rows > 0 caps
- * the grid rows per CTA of the x passes (0: no cap). */
-int fp_set_tiling(fp_handle h, int tile, int tma_off, int x_bulk, int x_rows);
+ * the grid rows per CTA of the x passes (0: no cap), lowreg != 0 selects the
+ * FP32 register-fed y/z kernels capped at 168 registers per thread. */
+int fp_set_tiling(fp_handle h, int tile, int tma_off, int x_bulk, int x_rows, int lowreg);
 
 /* Permeability tensors of `count` independent microstructures (the reference
  * runs PermeabilityRunner once per geometry).  Problem i has grid dims[3i..3i+2]

@@ -110,7 +110,7 @@ def test_set_tiling_reproduces_the_tuned_apply(gpu_lib):
         y0 = p.operator_apply(x)
     with PermeabilityProblem(mask.shape, precision="mixed") as q:
         q.set_geometry(mask)
-        q.set_tiling(t["tile"], t["tma"], t["x_bulk"], t["x_rows"])
+        q.set_tiling(t["tile"], t["tma"], t["x_bulk"], t["x_rows"], t["lowreg"])
         y1 = q.operator_apply(x)
         with pytest.raises(Exception):
             q.set_tiling(7, True, True)
