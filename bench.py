@@ -62,7 +62,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--mode", default="solve",
                     choices=["solve", "apply", "batch", "learned", "brinkman"],
-                    help="apply: only run --reps operator applies per precision (for profilers)")
+                    help="solve: the headline (seconds to K at 256^3); apply: --reps operator "
+                         "applies per precision (for profilers); batch: 64 uneven "
+                         "microstructures; brinkman: the C2 Brinkman cell; learned: the "
+                         "learned warm start")
     ap.add_argument("--precision", default="mixed,fp64", help="precisions for --mode apply")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--tiling", default="",
