@@ -18,6 +18,7 @@ Masks are uint8 arrays of shape (nz, ny, nx), x fastest, 1 = fluid and
 """
 from __future__ import annotations
 
+import re
 import struct
 
 import numpy as np
@@ -120,3 +121,66 @@ def read_fgeo(path: str) -> np.ndarray:
     if len(data) != 32 + count * np.dtype(dt).itemsize:
         raise ValueError(".fgeo payload size mismatch: " + path)
     return np.frombuffer(data, dtype=dt, offset=32).astype(np.uint32).reshape(nz, ny, nx)
+
+
+_LEADING_INT = re.compile(r"\s*([+-]?\d+)")
+
+
+def _strip_comment(line: str) -> str:
+    cut = min((i for i in (line.find("#"), line.find(";")) if i >= 0), default=-1)
+    return line if cut < 0 else line[:cut]
+
+
+def _line_ints(line: str):
+    """The integers a C++ ``istringstream >> int`` loop reads from a line:
+    leading integer tokens, up to the first token that is not one."""
+    pos = 0
+    while True:
+        m = _LEADING_INT.match(line, pos)
+        if not m:
+            return
+        yield int(m.group(1))
+        pos = m.end()
+
+
+def read_geom_text(path: str) -> np.ndarray:
+    """Read the reference's text geometry (src/io/VoxelIO.cpp:47-86): '#' and
+    ';' start comments, the first non-empty line gives nx ny nz, then one
+    integer material id per voxel (x fastest) in any line layout; values past
+    nx*ny*nz are ignored.  Returns int64 material ids of shape (nz, ny, nx)."""
+    with open(path) as f:
+        lines = iter(f.read().splitlines())
+    dims = None
+    for line in lines:
+        body = _strip_comment(line)
+        if not body.strip():
+            continue
+        dims = list(_line_ints(body))[:3]
+        break
+    if dims is None or len(dims) < 3 or min(dims) < 0:
+        raise ValueError("VoxelIO::load_text expected first non-comment line: nx ny nz")
+    nx, ny, nz = dims
+    count = nx * ny * nz
+    vals = []
+    for line in lines:
+        if len(vals) >= count:
+            break
+        for v in _line_ints(_strip_comment(line)):
+            vals.append(v)
+            if len(vals) == count:
+                break
+    if len(vals) < count:
+        raise ValueError("VoxelIO::load_text insufficient voxel values")
+    return np.asarray(vals, dtype=np.int64).reshape(nz, ny, nx)
+
+
+def load_ids(path: str) -> np.ndarray:
+    """Material ids from a geometry file, by extension as the reference's
+    VoxelIO::load does (src/io/VoxelIO.cpp:159-164): ``.fgeo`` is binary,
+    anything else text."""
+    return read_fgeo(path) if path.endswith(".fgeo") else read_geom_text(path)
+
+
+def load_mask(path: str, fluid_id: int = FLUID_ID) -> np.ndarray:
+    """VoxelIO::load: the fluid mask (1 where the id equals ``fluid_id``)."""
+    return (load_ids(path) == fluid_id).astype(np.uint8)

@@ -361,6 +361,13 @@ class PermeabilityTensor:
     def data(self) -> np.ndarray:
         return self.k
 
+    def to_string(self, indent: str = "") -> str:
+        """src/post/PermeabilityTensor.cpp:20-28: rows in scientific notation
+        with 6 digits, two spaces between entries, rows joined by newline +
+        indent."""
+        rows = ["  ".join("%.6e" % self.k[3 * r + c] for c in range(3)) for r in range(3)]
+        return ("\n" + indent).join(rows)
+
 
 # ---------------------------------------------------------------------------
 # Brinkman penalisation (include/brinkman/FluidBrinkman.hpp:45-55)
