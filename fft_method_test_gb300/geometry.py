@@ -126,7 +126,8 @@ def read_fgeo(path: str) -> np.ndarray:
 _LEADING_INT = re.compile(r"\s*([+-]?\d+)")
 
 
-def _strip_comment(line: str) -> str:
+def strip_comment(line: str) -> str:
+    """The part of a line before its first "#" or ";" (the reference's comment rule)."""
     cut = min((i for i in (line.find("#"), line.find(";")) if i >= 0), default=-1)
     return line if cut < 0 else line[:cut]
 
@@ -152,7 +153,7 @@ def read_geom_text(path: str) -> np.ndarray:
         lines = iter(f.read().splitlines())
     dims = None
     for line in lines:
-        body = _strip_comment(line)
+        body = strip_comment(line)
         if not body.strip():
             continue
         dims = list(_line_ints(body))[:3]
@@ -165,7 +166,7 @@ def read_geom_text(path: str) -> np.ndarray:
     for line in lines:
         if len(vals) >= count:
             break
-        for v in _line_ints(_strip_comment(line)):
+        for v in _line_ints(strip_comment(line)):
             vals.append(v)
             if len(vals) == count:
                 break

@@ -86,9 +86,11 @@ class SimulationConfig:
     brinkman_method: str = "jacobi"           # | "fixed_point"
 
     @classmethod
-    def from_file(cls, path: str) -> "SimulationConfig":
-        """SimulationConfig::from_cli's --config step (SimulationConfig.cpp:318-330):
-        legacy keys first, then the hierarchical sections override them."""
+    def from_file(cls, path: str, **overrides) -> "SimulationConfig":
+        """SimulationConfig::from_cli (SimulationConfig.cpp:305-439): the
+        --config file (legacy keys first, then the hierarchical sections
+        override them), then ``overrides`` (field name -> value, in the place
+        of the command-line flags), then ``validate``."""
         cfg = cls()
         m = parse_config_file(path)
         _apply_global(cfg, m)
@@ -100,7 +102,35 @@ class SimulationConfig:
         _apply_bignonnet(cfg, m, "fluid.bignonnet")
         _apply_brinkman(cfg, m, "fluid.brinkman")
         _apply_gpu(cfg, m)
+        for key, val in overrides.items():
+            if not hasattr(cfg, key):
+                raise ValueError("Unknown option: " + key)
+            setattr(cfg, key, val)
+        cfg.validate()
         return cfg
+
+    def validate(self) -> None:
+        """The checks that end from_cli (SimulationConfig.cpp:407-436); an
+        unset ``fft_threads`` inherits ``threads`` (at least 1)."""
+        if self.fft_threads == 0:
+            self.fft_threads = self.threads or 1
+        if self.analysis != "fluid":
+            raise ValueError("analysis must be 'fluid' (other analyses are not implemented yet)")
+        if self.solver not in ("bignonnet", "brinkman"):
+            raise ValueError("solver must be 'bignonnet' or 'brinkman'")
+        if self.fluid_mode == "pressure_gradient" and not any(self.pressure_gradient):
+            raise ValueError("pressure_gradient must be non-zero when fluid mode is "
+                             "pressure_gradient")
+        checks = ((self.mu_explicit and self.mu <= 0.0, "mu must be positive"),
+                  (self.voxel_size <= 0.0, "voxel_size must be > 0"),
+                  (self.tolerance <= 0.0, "tolerance must be positive"),
+                  (self.max_iterations == 0, "max_iterations must be >= 1"),
+                  (self.fft_threads <= 0, "fft_threads must be >= 1"),
+                  (self.threads < 0, "threads must be >= 0"),
+                  (self.p_radius < 0, "p_radius must be >= 0"))
+        for bad, msg in checks:
+            if bad:
+                raise ValueError(msg)
 
 
 def _trim(s: str) -> str:
@@ -119,7 +149,7 @@ def parse_config_file(path: str) -> dict:
     section = ""
     with f:
         for line_no, line in enumerate(f.read().split("\n"), start=1):
-            line = _trim(G._strip_comment(line))
+            line = _trim(G.strip_comment(line))
             if not line:
                 continue
             if line[0] == "[":

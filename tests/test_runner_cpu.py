@@ -269,3 +269,75 @@ def test_run_dispatch_errors():
         R.run(R.SimulationConfig(material_file="mats.txt"))
     with pytest.raises(ValueError, match="Unknown solver"):
         R.run(R.SimulationConfig(solver="lbm"))
+
+
+def test_reference_config_test_cases(tmp_path):
+    """The assertions of the reference's tests/test_simulation_config.cpp,
+    command-line flags given as overrides."""
+    legacy = tmp_path / "legacy.cfg"
+    legacy.write_text("solver = brinkman\nthreads = 4\nmax_iterations = 321\n"
+                      "geometry_file = examples/sample_inputs/geometry.geom\n\n"
+                      "[bignonnet]\nfft_threads = 0\n\n[brinkman]\ntolerance = 1e-6\n")
+    c = R.SimulationConfig.from_file(str(legacy))
+    assert c.solver == "brinkman" and c.threads == 4 and c.fft_threads == 4
+    assert c.max_iterations == 321 and c.brinkman_tolerance == 1e-6
+    c = R.SimulationConfig.from_file(str(legacy), threads=6, fft_threads=2)
+    assert c.threads == 6 and c.fft_threads == 2
+
+    schema = tmp_path / "schema.cfg"
+    schema.write_text("solver = bignonnet\n\n[analysis]\ntype = fluid\n\n[fluid]\n"
+                      "mode = pressure_gradient\nsolver = brinkman\ncompute_backend = gpu\n"
+                      "pressure_gradient = 0.0, 2.5, -1.0\nthreads = 3\nfft_threads = 0\n"
+                      "write_velocity_fields = true\nmax_iterations = 120\ntolerance = 2e-7\n\n"
+                      "[fluid.brinkman]\ntolerance = 3e-7\nforcing_magnitude = 4.0\n")
+    c = R.SimulationConfig.from_file(str(schema))
+    assert c.analysis == "fluid" and c.fluid_mode == "pressure_gradient"
+    assert c.solver == "brinkman" and c.compute_backend == "gpu"
+    assert c.threads == 3 and c.fft_threads == 3 and c.write_velocity_fields
+    assert c.max_iterations == 120 and c.tolerance == 2e-7
+    assert c.brinkman_tolerance == 3e-7 and c.brinkman_forcing_magnitude == 4.0
+    assert c.pressure_gradient == (0.0, 2.5, -1.0)
+    c = R.SimulationConfig.from_file(str(schema), fluid_mode="permeability", solver="bignonnet",
+                                     compute_backend="cpu")
+    assert (c.fluid_mode, c.solver, c.compute_backend) == ("permeability", "bignonnet", "cpu")
+
+    bad = tmp_path / "bad.cfg"
+    bad.write_text("[analysis]\ntype = fluid\n\n[fluid]\nmode = pressure_gradient\n"
+                   "pressure_gradient = 0, 0, 0\n")
+    with pytest.raises(ValueError, match="non-zero"):
+        R.SimulationConfig.from_file(str(bad))
+    bad.write_text("[analysis]\ntype = elastic\n")
+    with pytest.raises(ValueError, match="analysis must be 'fluid'"):
+        R.SimulationConfig.from_file(str(bad))
+
+
+@pytest.mark.parametrize("body, msg", [
+    ("solver = lbm\n", "solver must be"),
+    ("[fluid]\nmu = 0\n", "mu must be positive"),
+    ("voxel_size = -1\n", "voxel_size must be > 0"),
+    ("[fluid]\ntolerance = 0\n", "tolerance must be positive"),
+    ("max_iterations = 0\n", "max_iterations must be >= 1"),
+    ("threads = -2\n", "fft_threads must be >= 1"),   # inherits threads first
+    ("threads = -2\n[bignonnet]\nfft_threads = 2\n", "threads must be >= 0"),
+    ("[bignonnet]\np_radius = -1\n", "p_radius must be >= 0"),
+])
+def test_config_validation(tmp_path, body, msg):
+    p = tmp_path / "v.cfg"
+    p.write_text(body)
+    with pytest.raises(ValueError, match=msg):
+        R.SimulationConfig.from_file(str(p))
+
+
+def test_reference_voxelio_test_cases(tmp_path):
+    """The assertions of the reference's tests/test_voxelio_load_geometry.cpp."""
+    import struct
+
+    t = tmp_path / "geometry.geom"
+    t.write_text("# comment\n2 2 1\n0 5\n9 0\n")
+    ids = G.load_ids(str(t))
+    assert ids.shape == (1, 2, 2) and ids.ravel().tolist() == [0, 5, 9, 0]
+    f = tmp_path / "geometry.fgeo"
+    f.write_bytes(b"FGEO" + bytes([1, 2, 0, 0]) + struct.pack("<3Q", 2, 2, 1)
+                  + struct.pack("<4H", 1, 7, 9, 1))
+    ids = G.load_ids(str(f))
+    assert ids.shape == (1, 2, 2) and ids.ravel().tolist() == [1, 7, 9, 1]
