@@ -473,17 +473,7 @@ def batch_workload(count: int = 64):
     with correlation length 6."""
     from fft_method_test_gb300 import geometry as G
 
-    masks = []
-    for i in range(count):
-        seed = 2000 + i
-        rng = np.random.default_rng(seed)
-        edge = int(rng.choice([48, 64, 80, 96, 128, 160]))
-        phi = float(rng.uniform(0.3, 0.8))
-        if seed % 2 == 0:
-            masks.append(G.spheres(edge, 3.0, phi, seed=seed, radius_max=10.0))
-        else:
-            masks.append(G.gaussian_field(edge, 6.0, phi, seed=seed))
-    return masks
+    return [G.batch_cell(2000 + i) for i in range(count)]
 
 
 def run_batch(args):

@@ -467,6 +467,7 @@ int fp::create_handle(int nx, int ny, int nz, double voxel_size, double mu, int 
         P.x_bulk = !P.tma_off;
     }
     if (const char* t = std::getenv("FFTPERM_NO_GRAPHS")) P.use_graphs = std::atoi(t) == 0;
+    if (const char* t = std::getenv("FFTPERM_NO_FAST")) P.fast_off = std::atoi(t) != 0;
     if (const char* t = std::getenv("FFTPERM_AHEAD")) {
         const double f = std::atof(t);
         if (f > 0.0 && f < 1.0) P.ahead_factor = f;

@@ -1,0 +1,87 @@
+// fast_dispatch.cu -- host side of the specialised apply passes
+// (fft_fast.cuh): when they apply, launch geometry, and the pass sequence.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "fft_fast.cuh"
+
+namespace fp {
+
+bool fast_apply_supported(const Problem& P, int precision, int src_kind, int dst_kind, int stage) {
+    (void)precision;
+    if (P.fast_off) return false;
+    if (src_kind != kSrcCompact || dst_kind != kDstCompact || stage != kStageFull) return false;
+    return fast::edge_supported(P.nx) && fast::edge_supported(P.ny) && fast::edge_supported(P.nz);
+}
+
+template <typename T>
+static cudaError_t fast_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
+    using T2 = c_t<T>;
+    fast::FastArgs a{};
+    a.nx = P.nx;
+    a.ny = P.ny;
+    a.nz = P.nz;
+    a.nxh = P.nxh;
+    a.rs = P.rs;
+    a.nh = P.nh;
+    a.nrows = P.nrows;
+    a.n = P.n;
+    a.plane = (long long)P.ny * P.rs;
+    a.tw32x = P.px.tw32;
+    a.tw32y = P.py.tw32;
+    a.tw32z = P.pz.tw32;
+    a.tw64x = P.px.tw64;
+    a.tw64y = P.py.tw64;
+    a.tw64z = P.pz.tw64;
+    a.spec = P.d_spec;
+    a.green = sizeof(T) == 8 ? (const void*)P.d_green64 : (const void*)P.d_green32;
+    a.support = P.d_support;
+    a.row_ptr = P.d_row_ptr;
+    a.src = aa.src;
+    a.src_sum = aa.src_sum;
+    a.inv_nb = P.nb > 0 ? 1.0 / (double)P.nb : 0.0;
+    a.dst = aa.dst;
+    a.dot_with = aa.dot_with;
+    a.scale = 1.0 / (double)P.n;
+    a.partials = P.d_partials;
+    a.skip = aa.skip;
+
+    // x passes: tiles of `rows` grid rows, persistent over the tiles
+    int rows = fast::x_rows_for(P.nx);
+    if (rows > P.nrows) rows = (int)((P.nrows + 1) & ~1LL);
+    a.rows = rows;
+    a.ntiles = (P.nrows + rows - 1) / rows;
+    const int xthreads = ((3 * rows / 2 * fast::x_tpl(P.nx) + 31) / 32) * 32;
+    const size_t xsmem = (size_t)(3 * rows / 2) * fast::x_ld_rt<T>(P.nx) * sizeof(T2);
+    const int fwd_per_sm = fast::x_blocks_per_sm<T>(P.nx, false, xthreads, xsmem);
+    const int inv_per_sm = fast::x_blocks_per_sm<T>(P.nx, true, xthreads, xsmem);
+    const int xgrid_f = (int)std::min<long long>(a.ntiles, (long long)fwd_per_sm * P.sm_count);
+    int xgrid_i = (int)std::min<long long>(a.ntiles, (long long)inv_per_sm * P.sm_count);
+    xgrid_i = std::min(xgrid_i, kMaxPartials);
+
+    // column passes
+    constexpr int TX = fast::col_tx<T>();
+    const int ntx = (P.nxh + TX - 1) / TX;
+    const dim3 ygrid(ntx, P.nz, 3);
+    const dim3 zgrid(ntx, P.ny, 1);
+    const size_t zsmem = (size_t)3 * TX * fast::col_ld_rt<T>(P.nz) * sizeof(T2) +
+                         (size_t)6 * P.nz * TX * sizeof(T);
+
+    cudaStream_t st = P.stream;
+    cudaError_t e;
+    if ((e = fast::run_xfwd<T>(P.nx, a, xgrid_f, xthreads, xsmem, st)) != cudaSuccess) return e;
+    if ((e = fast::run_y<T>(P.ny, -1, a, ygrid, st)) != cudaSuccess) return e;
+    if ((e = fast::run_z<T>(P.nz, a, zgrid, zsmem, st)) != cudaSuccess) return e;
+    if ((e = fast::run_y<T>(P.ny, +1, a, ygrid, st)) != cudaSuccess) return e;
+    if ((e = fast::run_xinv<T>(P.nx, a, xgrid_i, xthreads, xsmem, st)) != cudaSuccess) return e;
+    *nparts = xgrid_i;
+    return cudaSuccess;
+}
+
+cudaError_t fast_apply(Problem& P, int precision, const ApplyArgs& aa, int* nparts) {
+    if (precision == kFP64) return fast_impl<double>(P, aa, nparts);
+    return fast_impl<float>(P, aa, nparts);
+}
+
+}  // namespace fp

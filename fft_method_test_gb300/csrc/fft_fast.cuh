@@ -1,0 +1,585 @@
+// fft_fast.cuh -- the five apply passes specialised at compile time for the
+// power-of-two grid edges 32, 64, 128 and 256, for compact-vector operator
+// applies (scatter in, gather out).  The generic engine of fft_passes.cuh serves every other edge,
+// source and destination.
+//
+// Each line of length N = R1 * R2 is transformed by TPL = R2 threads with the
+// four-step decomposition, one vector component per thread:
+//
+//   x[R2*i + a]  (i < R1, a < R2)
+//   stage A  thread owning a: DFT-R1 over i, times W_N^(S a k)  -> Y[k][a]
+//   stage B  thread owning k: DFT-R2 over a                      -> X[k + R1*m]
+//
+// The inverse runs the same two stages with the radices swapped (R2 first),
+// so its stage A starts from exactly the values stage B of the forward
+// transform leaves with each owner: the z pass multiplies by the Green tensor
+// between the two without another exchange.  Only the Y exchange between the
+// stages (and the natural-order exchange around the Green multiply) goes
+// through shared memory; every stage reads or writes HBM directly where its
+// owner pattern is the natural one.
+//
+// Passes (kernels below):
+//   k_fx_fwd   scatter of the compact vector (minus its mean) into real
+//              x-lines, two real lines per complex FFT, half spectrum out
+//   k_fcol     y pass, one component per CTA slice, TX kx columns per CTA
+//   k_fz       z pass: forward, 3x3 Green multiply, inverse, all three
+//              components in one CTA; the Green tile is prefetched into
+//              shared memory with cp.async while the forward transform runs
+//   k_fx_inv   C2R x lines, gather to the support, 1/N scale, per-CTA partial
+//              sums (component sums and the dot with a given vector)
+//
+// Shared-memory line strides are chosen so that the half-warp (FP32) or
+// quarter-warp (FP64) of every exchange touches distinct banks.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "fft_engine.cuh"
+#include "internal.h"
+
+namespace fp {
+namespace fast {
+
+// N = R1 * R2 with R1 >= R2; TPL = R2 threads per line.
+template <int N>
+struct Split;
+template <>
+struct Split<32> {
+    static constexpr int R1 = 8, R2 = 4;
+};
+template <>
+struct Split<64> {
+    static constexpr int R1 = 8, R2 = 8;
+};
+template <>
+struct Split<128> {
+    static constexpr int R1 = 16, R2 = 8;
+};
+template <>
+struct Split<256> {
+    static constexpr int R1 = 16, R2 = 16;
+};
+
+// ---- small DFTs in natural order -------------------------------------------
+
+// Natural-order DFT of R values (S = -1 forward, +1 backward) with the
+// radix kernels of fft_engine.cuh (2, 3, 4, 5, 8, 16).
+template <int R, int S, typename T2>
+__device__ __forceinline__ void dft_nat(T2 (&v)[R]) {
+    T2 t[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) t[i] = v[i];
+    dft_r<R, S>(t);
+#pragma unroll
+    for (int k = 0; k < R; ++k) v[k] = t[out_slot<R>(k)];
+}
+
+// twiddle W_N^(S e) from the table tw[j] = exp(-2 pi i j / N), 0 <= e < N
+template <int S, typename T2>
+__device__ __forceinline__ T2 twiddle(const T2* __restrict__ tw, int e) {
+    T2 w = __ldg(tw + e);
+    if (S > 0) w.y = -w.y;
+    return w;
+}
+
+// ---- line strides ------------------------------------------------------------
+
+// Positions used in a line: the natural N plus the Y layout k*(RB+1) + a of
+// either direction (RB = R2 forward, R1 inverse).
+template <int N>
+__host__ __device__ constexpr int line_span() {
+    return N + Split<N>::R1;
+}
+
+// Column passes (thread = column + TX * (owner + TPL * comp)): FP32 lines
+// need stride = 2 mod 16 elements (a half-warp = 8 columns x 2 owners),
+// FP64 lines an odd stride (a quarter-warp = TX <= 8 columns of one owner).
+template <int N, typename T>
+__host__ __device__ constexpr int col_ld() {
+    return sizeof(T) == 4 ? ((line_span<N>() + 13) / 16) * 16 + 2 : (line_span<N>() | 1);
+}
+
+// x passes (thread = owner + TPL * line): the lines of one half-warp (FP32)
+// or quarter-warp (FP64) must fall in distinct banks, so for a power-of-two
+// TPL below the group size G the stride is TPL mod G.
+template <int N, typename T>
+__host__ __device__ constexpr int x_ld() {
+    constexpr int G = sizeof(T) == 4 ? 16 : 8;
+    constexpr int tpl = Split<N>::R2;
+    constexpr int base = ((line_span<N>() + G - 1) / G) * G;
+    return tpl < G ? base + tpl : base;
+}
+
+// ---- four-step stages --------------------------------------------------------
+
+// Stage A for owners a = t + TPL*j (j < RB/TPL): loads RA values through
+// load(pos) (pos = RB*i + a), DFT-RA, twiddle W_N^(S a k), stores Y[k][a] at
+// line[k*(RB+1) + a].  With SYNC the CTA synchronises between the loads and
+// the stores (the loads read the same lines).
+template <int RA, int RB, int S, int TPL, bool SYNC, typename T2, class Load>
+__device__ __forceinline__ void stage_a(T2* line, int t, bool active, const T2* __restrict__ tw,
+                                        Load& load) {
+    constexpr int J = RB / TPL;
+    T2 v[J][RA];
+#pragma unroll
+    for (int j = 0; j < J; ++j)
+#pragma unroll
+        for (int i = 0; i < RA; ++i) v[j][i] = active ? load(RB * i + t + TPL * j) : T2{};
+    if (SYNC) __syncthreads();
+    if (active) {
+#pragma unroll
+        for (int j = 0; j < J; ++j) {
+            const int a = t + TPL * j;
+            dft_nat<RA, S>(v[j]);
+#pragma unroll
+            for (int k = 0; k < RA; ++k) {
+                T2 y = v[j][k];
+                if (k > 0) y = cmul(y, twiddle<S>(tw, a * k));  // a * k < N
+                line[k * (RB + 1) + a] = y;
+            }
+        }
+    }
+}
+
+// Stage B for owners k = t + TPL*j (j < RA/TPL): loads Y[k][a] (a < RB),
+// DFT-RB, hands X[k + RA*m] to store(pos, value).  With SYNC the CTA
+// synchronises between the loads and the stores.
+template <int RA, int RB, int S, int TPL, bool SYNC, typename T2, class Store>
+__device__ __forceinline__ void stage_b(const T2* line, int t, bool active, Store& store) {
+    constexpr int J = RA / TPL;
+    T2 u[J][RB];
+#pragma unroll
+    for (int j = 0; j < J; ++j)
+#pragma unroll
+        for (int a = 0; a < RB; ++a)
+            u[j][a] = active ? line[(t + TPL * j) * (RB + 1) + a] : T2{};
+    if (SYNC) __syncthreads();
+    if (active) {
+#pragma unroll
+        for (int j = 0; j < J; ++j) {
+            const int k = t + TPL * j;
+            dft_nat<RB, S>(u[j]);
+#pragma unroll
+            for (int m = 0; m < RB; ++m) store(k + RA * m, u[j][m]);
+        }
+    }
+}
+
+// ---- kernel arguments ----------------------------------------------------------
+
+struct FastArgs {
+    int nx, ny, nz, nxh;
+    long long rs, nh, nrows, n, plane;
+    const float2* tw32x;
+    const float2* tw32y;
+    const float2* tw32z;
+    const double2* tw64x;
+    const double2* tw64y;
+    const double2* tw64z;
+    void* spec;
+    const void* green;
+    // x passes
+    int rows;       // grid rows per tile (even)
+    long long ntiles;
+    const int* support;
+    const int* row_ptr;
+    const double* src;
+    const double* src_sum;
+    double inv_nb;
+    double* dst;
+    const double* dot_with;
+    double scale;
+    double* partials;
+    const int* skip;
+};
+
+template <typename T>
+__device__ __forceinline__ const c_t<T>* tw_of(const FastArgs& a, int axis);
+template <>
+__device__ __forceinline__ const float2* tw_of<float>(const FastArgs& a, int axis) {
+    return axis == 0 ? a.tw32x : (axis == 1 ? a.tw32y : a.tw32z);
+}
+template <>
+__device__ __forceinline__ const double2* tw_of<double>(const FastArgs& a, int axis) {
+    return axis == 0 ? a.tw64x : (axis == 1 ? a.tw64y : a.tw64z);
+}
+
+// threads of the x passes for `rows` grid rows per tile: 3*rows/2 complex
+// lines of TPL threads, rounded up to whole warps
+template <int N>
+__host__ __device__ constexpr int x_threads(int rows) {
+    return ((3 * rows / 2 * Split<N>::R2 + 31) / 32) * 32;
+}
+
+// ---- P1: scatter + R2C x -------------------------------------------------------
+
+template <typename T, int N>
+__global__ void __launch_bounds__(384) k_fx_fwd(FastArgs a) {
+    if (a.skip && *a.skip) return;
+    using T2 = c_t<T>;
+    constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = R2;
+    constexpr int LD = x_ld<N, T>();
+    constexpr int NH = N / 2 + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T2* lines = reinterpret_cast<T2*>(smem_raw);
+    const int RB = a.rows;
+    const int nq = 3 * RB / 2;
+    const int tid = threadIdx.x;
+    const int nthr = blockDim.x;
+    const int q = tid / TPL;
+    const int t = tid - q * TPL;
+    const T2* tw = tw_of<T>(a, 0);
+    T2* spec = reinterpret_cast<T2*>(a.spec);
+    const T mean[3] = {a.src_sum ? (T)(a.src_sum[0] * a.inv_nb) : (T)0,
+                       a.src_sum ? (T)(a.src_sum[1] * a.inv_nb) : (T)0,
+                       a.src_sum ? (T)(a.src_sum[2] * a.inv_nb) : (T)0};
+    for (long long tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const long long r0 = tile * RB;
+        const int rows = (int)min((long long)RB, a.nrows - r0);
+        const int nreal = 3 * rows;
+        const int nqa = (nreal + 1) / 2;
+        // 1) zero the lines
+        for (int i = tid; i < nq * LD; i += nthr) lines[i] = T2{};
+        __syncthreads();
+        // 2) scatter the compact vector minus its mean (support voxels only)
+        {
+            const int s0 = a.row_ptr[r0];
+            const int s1 = a.row_ptr[r0 + rows];
+            for (int s = s0 + tid; s < s1; s += nthr) {
+                const int idx = a.support[s];
+                const int row = idx / N;
+                const int x = idx - row * N;
+                const int rl = row - (int)r0;
+                const double c0 = a.src[3LL * s], c1 = a.src[3LL * s + 1], c2 = a.src[3LL * s + 2];
+                const T v3[3] = {(T)c0 - mean[0], (T)c1 - mean[1], (T)c2 - mean[2]};
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const int L = 3 * rl + c;
+                    T2* p = &lines[(L >> 1) * LD + x];
+                    if (L & 1) p->y = v3[c]; else p->x = v3[c];
+                }
+            }
+        }
+        __syncthreads();
+        // 3) forward FFT of every complex line (stage A reads the natural line,
+        //    stage B leaves X in registers, written back in natural order)
+        const bool act = q < nqa;
+        T2* my = lines + (act ? q : 0) * LD;
+        {
+            auto ld_nat = [&](int pos) { return my[pos]; };
+            stage_a<R1, R2, -1, TPL, true>(my, t, act, tw, ld_nat);
+            __syncthreads();
+            auto st_nat = [&](int pos, T2 v) { my[pos] = v; };
+            stage_b<R1, R2, -1, TPL, true>(my, t, act, st_nat);
+        }
+        __syncthreads();
+        // 4) separate the two real spectra of each complex line, store the half spectra
+        for (int it = tid; it < nqa * NH; it += nthr) {
+            const int qq = it / NH;
+            const int k = it - qq * NH;
+            const T2 zk = lines[qq * LD + k];
+            const T2 zn = lines[qq * LD + (k == 0 ? 0 : N - k)];
+            const T h = (T)0.5;
+            const T2 A = cmk<T2>(h * (zk.x + zn.x), h * (zk.y - zn.y));
+            const T2 B = cmk<T2>(h * (zk.y + zn.y), h * (zn.x - zk.x));
+            const int La = 2 * qq, rla = La / 3, ca = La - 3 * rla;
+            spec[ca * a.nh + (r0 + rla) * a.rs + k] = A;
+            const int Lb = La + 1;
+            if (Lb < nreal) {
+                const int rlb = Lb / 3, cb = Lb - 3 * rlb;
+                spec[cb * a.nh + (r0 + rlb) * a.rs + k] = B;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---- P5: C2R x + gather + partial sums -------------------------------------------
+
+template <typename T, int N>
+__global__ void __launch_bounds__(384) k_fx_inv(FastArgs a) {
+    if (a.skip && *a.skip) return;
+    using T2 = c_t<T>;
+    constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = R2;
+    constexpr int LD = x_ld<N, T>();
+    constexpr int NH = N / 2 + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double red[4 * 32];
+    T2* lines = reinterpret_cast<T2*>(smem_raw);
+    const int RB = a.rows;
+    const int tid = threadIdx.x;
+    const int nthr = blockDim.x;
+    const int q = tid / TPL;
+    const int t = tid - q * TPL;
+    const T2* tw = tw_of<T>(a, 0);
+    const T2* spec = reinterpret_cast<const T2*>(a.spec);
+    const T scale = (T)a.scale;
+    T acc[4] = {(T)0, (T)0, (T)0, (T)0};
+    for (long long tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const long long r0 = tile * RB;
+        const int rows = (int)min((long long)RB, a.nrows - r0);
+        const int nreal = 3 * rows;
+        const int nqa = (nreal + 1) / 2;
+        // 1) complex lines Z = A + iB from the two Hermitian half spectra
+        for (int it = tid; it < nqa * NH; it += nthr) {
+            const int qq = it / NH;
+            const int k = it - qq * NH;
+            const int La = 2 * qq, rla = La / 3, ca = La - 3 * rla;
+            T2 A = spec[ca * a.nh + (r0 + rla) * a.rs + k];
+            T2 B = T2{};
+            const int Lb = La + 1;
+            if (Lb < nreal) {
+                const int rlb = Lb / 3, cb = Lb - 3 * rlb;
+                B = spec[cb * a.nh + (r0 + rlb) * a.rs + k];
+            }
+            if (k == 0 || (N % 2 == 0 && 2 * k == N)) {  // DC and Nyquist are real
+                A.y = (T)0;
+                B.y = (T)0;
+            }
+            lines[qq * LD + k] = cmk<T2>(A.x - B.y, A.y + B.x);
+            if (k > 0 && N - k >= NH) lines[qq * LD + (N - k)] = cmk<T2>(A.x + B.y, B.x - A.y);
+        }
+        __syncthreads();
+        // 2) inverse FFT (radices swapped: R2 first), result in natural order
+        const bool act = q < nqa;
+        T2* my = lines + (act ? q : 0) * LD;
+        {
+            auto ld_nat = [&](int pos) { return my[pos]; };
+            stage_a<R2, R1, +1, TPL, true>(my, t, act, tw, ld_nat);
+            __syncthreads();
+            auto st_nat = [&](int pos, T2 v) { my[pos] = v; };
+            stage_b<R2, R1, +1, TPL, true>(my, t, act, st_nat);
+        }
+        __syncthreads();
+        // 3) gather to the support with the 1/N scale, partial sums
+        {
+            const int s0 = a.row_ptr[r0];
+            const int s1 = a.row_ptr[r0 + rows];
+            for (int s = s0 + tid; s < s1; s += nthr) {
+                const int idx = a.support[s];
+                const int row = idx / N;
+                const int x = idx - row * N;
+                const int rl = row - (int)r0;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const int L = 3 * rl + c;
+                    const T2 zv = lines[(L >> 1) * LD + x];
+                    const T val = ((L & 1) ? zv.y : zv.x) * scale;
+                    a.dst[3LL * s + c] = (double)val;
+                    acc[c] += val;
+                    if (a.dot_with) acc[3] += (T)a.dot_with[3LL * s + c] * val;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    double accd[4] = {(double)acc[0], (double)acc[1], (double)acc[2], (double)acc[3]};
+    double out[4];
+    block_sum<4>(accd, red, out);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) a.partials[4LL * blockIdx.x + i] = out[i];
+    }
+}
+
+// ---- P2 / P4: y pass -------------------------------------------------------------
+
+// One CTA: TX kx columns of one z plane for one component (blockIdx.z).
+template <typename T, int N, int S, int TX>
+__global__ void __launch_bounds__(TX * Split<N>::R2) k_fcol_y(FastArgs a) {
+    if (a.skip && *a.skip) return;
+    using T2 = c_t<T>;
+    constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = R2;
+    constexpr int LD = col_ld<N, T>();
+    __shared__ __align__(16) T2 lines[TX * LD];
+    const int c = threadIdx.x % TX;
+    const int t = threadIdx.x / TX;
+    const int k0 = blockIdx.x * TX;
+    const bool act = k0 + c < a.nxh;
+    const T2* tw = tw_of<T>(a, 1);
+    T2* base = reinterpret_cast<T2*>(a.spec) + blockIdx.z * a.nh + (long long)blockIdx.y * N * a.rs +
+               k0 + (act ? c : 0);
+    const long long es = a.rs;
+    T2* my = lines + c * LD;
+    auto ld_g = [&](int pos) { return base[pos * es]; };
+    auto st_g = [&](int pos, T2 v) { base[pos * es] = v; };
+    if (S < 0) {
+        stage_a<R1, R2, -1, TPL, false>(my, t, act, tw, ld_g);
+        __syncthreads();
+        stage_b<R1, R2, -1, TPL, false>(my, t, act, st_g);
+    } else {
+        stage_a<R2, R1, +1, TPL, false>(my, t, act, tw, ld_g);
+        __syncthreads();
+        stage_b<R2, R1, +1, TPL, false>(my, t, act, st_g);
+    }
+}
+
+// ---- P3: z forward + Green + z inverse -------------------------------------------
+
+// cp.async of 8 bytes global -> shared (the FP32 Green rows are 8-byte aligned)
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(
+                     static_cast<uint32_t>(__cvta_generic_to_shared(smem))),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// One CTA: TX kx columns of one ky row, all three components
+// (thread = column + TX * (owner + TPL * comp)).
+template <typename T, int N, int TX>
+__global__ void __launch_bounds__(3 * TX * Split<N>::R2, 2) k_fz(FastArgs a) {
+    if (a.skip && *a.skip) return;
+    using T2 = c_t<T>;
+    constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = R2;
+    constexpr int LD = col_ld<N, T>();
+    constexpr int NT = 3 * TX * TPL;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T2* lines = reinterpret_cast<T2*>(smem_raw);          // [3][TX][LD]
+    T* gsm = reinterpret_cast<T*>(lines + 3 * TX * LD);   // [6][N][TX]
+    const int c = threadIdx.x % TX;
+    const int t = (threadIdx.x / TX) % TPL;
+    const int comp = threadIdx.x / (TX * TPL);
+    const int k0 = blockIdx.x * TX;
+    const bool act = k0 + c < a.nxh;
+    const long long ky = blockIdx.y;
+    const T2* tw = tw_of<T>(a, 2);
+    // Green tile prefetch: 6 components x N kz rows x TX columns
+    {
+        const T* g = reinterpret_cast<const T*>(a.green);
+        constexpr int PER = 8 / sizeof(T);  // elements per 8-byte copy
+        constexpr int CPR = TX / PER;       // copies per row
+        const int ncols = min(TX, a.nxh - k0);
+        for (int i = threadIdx.x; i < 6 * N * CPR; i += NT) {
+            const int part = i % CPR;
+            const int row = i / CPR;  // gc * N + kz
+            const int gc = row / N;
+            const int kz = row - gc * N;
+            T* dstp = gsm + (size_t)row * TX + part * PER;
+            if (part * PER < ncols) {
+                const T* srcp = g + gc * a.nh + kz * a.plane + ky * a.rs + k0 + part * PER;
+                if (part * PER + PER <= ncols || sizeof(T) == 8) {
+                    cp_async8(dstp, srcp);
+                } else {
+                    dstp[0] = srcp[0];  // the last column of an odd-width row
+                }
+            }
+        }
+        cp_async_commit();
+    }
+    T2* base = reinterpret_cast<T2*>(a.spec) + comp * a.nh + ky * a.rs + k0 + (act ? c : 0);
+    const long long es = a.plane;
+    T2* my = lines + (comp * TX + c) * LD;
+    // forward stage A from HBM, stage B back to the lines in natural order
+    {
+        auto ld_g = [&](int pos) { return base[pos * es]; };
+        stage_a<R1, R2, -1, TPL, false>(my, t, act, tw, ld_g);
+    }
+    __syncthreads();
+    {
+        auto st_nat = [&](int pos, T2 v) { my[pos] = v; };
+        stage_b<R1, R2, -1, TPL, true>(my, t, act, st_nat);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    // Green multiply while loading the inverse stage A (owner k1 = same owner)
+    {
+        const T2* lx = lines + (0 * TX + c) * LD;
+        const T2* ly = lines + (1 * TX + c) * LD;
+        const T2* lz = lines + (2 * TX + c) * LD;
+        // Green components of row `comp` of the symmetric tensor (xx xy xz yy yz zz)
+        const int g0 = comp == 0 ? 0 : (comp == 1 ? 1 : 2);
+        const int g1 = comp == 0 ? 1 : (comp == 1 ? 3 : 4);
+        const int g2 = comp == 0 ? 2 : (comp == 1 ? 4 : 5);
+        auto ld_green = [&](int pos) {
+            const T2 X = lx[pos], Y = ly[pos], Z = lz[pos];
+            const T a0 = gsm[((size_t)g0 * N + pos) * TX + c];
+            const T a1 = gsm[((size_t)g1 * N + pos) * TX + c];
+            const T a2 = gsm[((size_t)g2 * N + pos) * TX + c];
+            return cmk<T2>(a0 * X.x + a1 * Y.x + a2 * Z.x, a0 * X.y + a1 * Y.y + a2 * Z.y);
+        };
+        stage_a<R2, R1, +1, TPL, true>(my, t, act, tw, ld_green);
+    }
+    __syncthreads();
+    {
+        auto st_g = [&](int pos, T2 v) { base[pos * es] = v; };
+        stage_b<R2, R1, +1, TPL, false>(my, t, act, st_g);
+    }
+}
+
+}  // namespace fast
+
+// Runs the five passes with the specialised kernels when the grid, the
+// precision and the source/destination allow it; returns false (nothing
+// launched) otherwise.  Defined in fast_dispatch.cu.
+bool fast_apply_supported(const Problem& P, int precision, int src_kind, int dst_kind, int stage);
+cudaError_t fast_apply(Problem& P, int precision, const ApplyArgs& aa, int* nparts);
+
+}  // namespace fp
+
+// ---- launch runners (fast32.cu / fast64.cu) -------------------------------------
+
+namespace fp {
+namespace fast {
+
+// kx columns per CTA of the column passes: 64-byte row segments
+template <typename T>
+constexpr int col_tx() {
+    return sizeof(T) == 4 ? 8 : 4;
+}
+
+// grid edges with specialised kernels
+inline bool edge_supported(int n) { return n == 32 || n == 64 || n == 128 || n == 256; }
+
+// grid rows per tile of the x passes: about 192 threads per CTA
+inline int x_rows_for(int n) {
+    switch (n) {
+        case 32: return 32;
+        case 64: return 16;
+        case 128: return 16;
+        default: return 8;
+    }
+}
+inline int x_tpl(int n) {
+    switch (n) {
+        case 32: return Split<32>::R2;
+        case 64: return Split<64>::R2;
+        case 128: return Split<128>::R2;
+        default: return Split<256>::R2;
+    }
+}
+template <typename T>
+int x_ld_rt(int n) {
+    switch (n) {
+        case 32: return x_ld<32, T>();
+        case 64: return x_ld<64, T>();
+        case 128: return x_ld<128, T>();
+        default: return x_ld<256, T>();
+    }
+}
+template <typename T>
+int col_ld_rt(int n) {
+    switch (n) {
+        case 32: return col_ld<32, T>();
+        case 64: return col_ld<64, T>();
+        case 128: return col_ld<128, T>();
+        default: return col_ld<256, T>();
+    }
+}
+
+template <typename T>
+cudaError_t run_xfwd(int n, const FastArgs& a, int grid, int threads, size_t smem, cudaStream_t s);
+template <typename T>
+cudaError_t run_xinv(int n, const FastArgs& a, int grid, int threads, size_t smem, cudaStream_t s);
+template <typename T>
+cudaError_t run_y(int n, int dir, const FastArgs& a, dim3 grid, cudaStream_t s);
+template <typename T>
+cudaError_t run_z(int n, const FastArgs& a, dim3 grid, size_t smem, cudaStream_t s);
+// blocks of the x kernels resident per SM at this shared-memory size
+template <typename T>
+int x_blocks_per_sm(int n, bool inverse, int threads, size_t smem);
+
+}  // namespace fast
+}  // namespace fp

@@ -140,6 +140,7 @@ struct Problem {
     MinresGraph graphs[6];
     long long queued = 0;  // iterations queued since minres_start (buffer rotation)
     bool tma_off = false;      // FFTPERM_NO_TMA=1 selects the register-fed passes
+    bool fast_off = false;     // FFTPERM_NO_FAST=1: the generic passes for every edge
     bool x_bulk = true;        // inverse x pass fed by bulk copies (tuned)
     int x_rows = 0;            // cap on grid rows per CTA of the x passes (0 = none; tuned)
     bool yz_lowreg = false;    // FP32 register-fed y/z passes capped at 168 registers (tuned)

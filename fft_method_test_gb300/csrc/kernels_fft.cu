@@ -14,6 +14,7 @@
 #include <cmath>
 #include <string>
 
+#include "fft_fast.cuh"
 #include "fft_passes.cuh"
 
 namespace fp {
@@ -399,8 +400,10 @@ static cudaError_t apply_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
 
 cudaError_t launch_apply(Problem& P, const ApplyArgs& a, int* nparts) {
     const int prec = a.precision >= 0 ? a.precision : P.precision;
+    if (prec != kFP64 && !P.d_green32) return cudaErrorInvalidValue;
+    if (fast_apply_supported(P, prec, a.src_kind, a.dst_kind, a.stage))
+        return fast_apply(P, prec, a, nparts);
     if (prec == kFP64) return apply_impl<double>(P, a, nparts);
-    if (!P.d_green32) return cudaErrorInvalidValue;
     return apply_impl<float>(P, a, nparts);
 }
 

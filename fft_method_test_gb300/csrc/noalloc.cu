@@ -24,7 +24,15 @@
 // Set-up: the first call on a device, with that device current, resolves the
 // array's device address with cudaGetSymbolAddress (host code cannot use the
 // array's name as a device address).  That first call should come before any
-// stream capture on the device.
+// stream capture on the device.  The address is cached per device for the
+// life of the process: a caller that resets a device (cudaDeviceReset) must
+// not call this entry on that device afterwards, because the cached address
+// belongs to the destroyed context.
+//
+// Cost: nothing is cached between calls, so every call recomputes the
+// twiddles and the whole Green table, each point of which sums the full
+// (2P+2)^3 alias window, before the transforms.  At 64^3 with P = 2 that is
+// a few times the cost of the transforms themselves.
 #include <cuda_runtime.h>
 
 #include <mutex>

@@ -83,6 +83,22 @@ def gaussian_field(n, corr_len: float, porosity: float, seed: int):
     return fluid.reshape(shape)
 
 
+BATCH_EDGES = (48, 64, 80, 96, 128, 160)
+
+
+def batch_cell(seed: int) -> np.ndarray:
+    """One cell of the uneven-size batch workload: the edge is drawn uniformly
+    from BATCH_EDGES and the porosity uniformly from [0.3, 0.8] with
+    default_rng(seed); even seeds are overlapping spheres with radii uniform
+    in [3, 10], odd seeds Gaussian random fields of correlation length 6."""
+    rng = np.random.default_rng(seed)
+    edge = int(rng.choice(list(BATCH_EDGES)))
+    phi = float(rng.uniform(0.3, 0.8))
+    if seed % 2 == 0:
+        return spheres(edge, 3.0, phi, seed=seed, radius_max=10.0)
+    return gaussian_field(edge, 6.0, phi, seed=seed)
+
+
 def porosity(mask: np.ndarray) -> float:
     return float(np.count_nonzero(mask)) / mask.size
 

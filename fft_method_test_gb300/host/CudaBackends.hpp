@@ -3,7 +3,7 @@
 //
 // These classes are compiled INSIDE the reference's tree (they include its
 // headers: fft/IFFTBackend.hpp, solver/ILinearOperator.hpp, ...) and link
-// libfftperm.so.  Integration steps are described in INTEGRATION.md:
+// libfftperm.so:
 //   * CudaFFTBackend : IFFTBackend  -- registered by create_fft_backend for
 //     ComputeBackend::GPU (src/fft/FFTBackendFactory.cpp:23-30), so the
 //     reference's GreenOperator runs its FFTs on the GPU unchanged.

@@ -146,7 +146,10 @@ int fp_solve_permeability(fp_handle h, double tol, int64_t maxit, double K[9],
  * return FP_ERR_INVALID.  The array is
  * shared by all calls: calls that overlap on the GPU race and must be
  * serialised by the caller.  The first call on a device resolves the array's
- * address; make that first call before any stream capture. */
+ * address; make that first call before any stream capture.  The address stays
+ * cached for the process, so do not call this entry on a device after
+ * resetting it.  Every call recomputes the twiddles and the Green table (the
+ * full alias sum per point) before the transforms. */
 int fp_green_apply_noalloc(int nx, int ny, int nz, double voxel_size, double mu, int p_radius,
                            const double* d_force_soa, double* d_velocity_soa, void* stream);
 

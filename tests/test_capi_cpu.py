@@ -52,7 +52,8 @@ def test_cpp_adapters_compile_against_reference(precision):
     import shutil
     import subprocess
 
-    ref = "/root/reference"
+    from __graft_entry__ import REFERENCE_DIR as ref
+
     if not os.path.isdir(os.path.join(ref, "src")):
         pytest.skip("reference sources not present on this host")
     gxx = shutil.which("g++")

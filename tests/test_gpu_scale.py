@@ -1,0 +1,150 @@
+"""GPU parity at the configurations' scale, and against the reference-built
+golden fixtures directly.
+
+* Permeability tensors of cells of 64^3 to 160^3 (Gaussian random fields of
+  the benchmark's kind, batch cells of edges 96 and 160, the Brinkman cell)
+  against the CPU oracle's K, stored in tests/golden/oracle_k.npz by
+  tests/golden/make_oracle_k.py (the oracle is pinned bit for bit to the
+  reference build).  Both solves stop at a relative MINRES residual of 1e-10;
+  K agrees to 1e-9 relative (the solves' own residual level), and to 1e-6 for
+  mixed precision at tol 1e-7.
+* Operator applies on the specialised power-of-two passes against the oracle
+  (1e-12 FP64, 5e-6 mixed) and against the generic passes (FFTPERM_NO_FAST).
+* The reference-built fixtures of tests/golden/golden.npz (C1 K, the 16^3
+  apply and RHS, the non-cubic Green table) read straight into GPU checks.
+"""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from fft_method_test_gb300 import geometry as G
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_K = os.path.join(HERE, "golden", "oracle_k.npz")
+GOLDEN = os.path.join(HERE, "golden", "golden.npz")
+
+
+def problem(shape, **kw):
+    from fft_method_test_gb300.permeability import PermeabilityProblem
+
+    return PermeabilityProblem(shape, **kw)
+
+
+def fixture_case(name):
+    with np.load(ORACLE_K) as z:
+        if name + "_K" not in z.files:
+            pytest.fail("oracle fixture %s missing from %s" % (name, ORACLE_K))
+        shape = tuple(int(v) for v in z[name + "_shape"])
+        bits = z[name + "_mask_bits"]
+        mask = np.unpackbits(bits)[: int(np.prod(shape))].reshape(shape).astype(np.uint8)
+        sha = str(z[name + "_sha256"])
+        assert hashlib.sha256(mask.tobytes()).hexdigest() == sha
+        return mask, z[name + "_K"].copy(), float(z[name + "_tol"]), int(z[name + "_nb"])
+
+
+@pytest.mark.parametrize("name", ["grf64", "grf128", "c4_96_grf", "c4_160_sph", "c2_128_sph"])
+def test_permeability_at_scale_matches_oracle(gpu_lib, name):
+    mask, K_ref, tol, nb_ref = fixture_case(name)
+    with problem(mask.shape, precision="fp64") as p:
+        assert p.set_geometry(mask) == nb_ref
+        K, st = p.solve_permeability(tol, 20000)
+    assert all(s["converged"] for s in st), st
+    assert rel_err(K, K_ref) < 1e-9, (name, rel_err(K, K_ref))
+
+
+@pytest.mark.parametrize("name", ["grf128", "c4_160_sph"])
+def test_mixed_permeability_at_scale_within_1e6(gpu_lib, name):
+    mask, K_ref, _, _ = fixture_case(name)
+    with problem(mask.shape, precision="mixed") as p:
+        p.set_geometry(mask)
+        p.autotune()
+        K, st = p.solve_permeability(1e-7, 20000)
+    assert all(s["converged"] for s in st), st
+    assert rel_err(K, K_ref) < 1e-6, (name, rel_err(K, K_ref))
+
+
+@pytest.mark.parametrize("shape", [(32, 32, 32), (64, 64, 64), (128, 128, 128), (64, 32, 128),
+                                   (256, 128, 64)])
+def test_specialised_apply_matches_oracle(gpu_lib, restatement, shape):
+    """Power-of-two edges run the specialised passes: FP64 apply to 1e-12 and
+    mixed to FP32 accuracy against the oracle."""
+    mask = G.gaussian_field(shape, 4.0, 0.4, seed=sum(shape))
+    ctx = restatement.context(mask)
+    x = np.random.default_rng(5).uniform(-1, 1, 3 * ctx.nb)
+    y_ref = ctx.operator_apply(x)
+    ctx.close()
+    with problem(shape, precision="fp64") as p:
+        p.set_geometry(mask)
+        y = p.operator_apply(x)
+        assert rel_err(y, y_ref) < 1e-12
+        p.set_precision("mixed")
+        y32 = p.operator_apply(x)
+    assert rel_err(y32, y_ref) < 5e-6
+
+
+@pytest.mark.parametrize("precision,bar", [("fp64", 1e-13), ("mixed", 2e-6)])
+def test_specialised_passes_match_generic(gpu_lib, precision, bar):
+    shape = (64, 128, 64)
+    mask = G.gaussian_field(shape, 5.0, 0.35, seed=9)
+    x = None
+    out = []
+    for off in ("0", "1"):
+        os.environ["FFTPERM_NO_FAST"] = off
+        try:
+            with problem(shape, precision=precision) as p:
+                nb = p.set_geometry(mask)
+                if x is None:
+                    x = np.random.default_rng(2).uniform(-1, 1, 3 * nb)
+                out.append(p.operator_apply(x))
+        finally:
+            os.environ.pop("FFTPERM_NO_FAST", None)
+    assert rel_err(out[0], out[1]) < bar
+
+
+def _golden():
+    return np.load(GOLDEN)
+
+
+def _mask_from_bits(bits, n):
+    return np.unpackbits(bits)[: n ** 3].reshape(n, n, n).astype(np.uint8)
+
+
+def test_golden_c1_K_direct(gpu_lib):
+    """C1 (32^3 spheres r 4, porosity 0.60, seed 1001, tol 1e-10): the GPU K
+    against the K the reference build computed."""
+    g = _golden()
+    mask = _mask_from_bits(g["c1_mask_bits"], 32)
+    with problem(mask.shape) as p:
+        p.set_geometry(mask)
+        assert np.array_equal(p.support(), g["c1_support"])
+        K, st = p.solve_permeability(1e-10, 2000)
+    assert rel_err(K, g["c1_K"]) < 1e-10, rel_err(K, g["c1_K"])
+
+
+def test_golden_op16_apply_and_rhs_direct(gpu_lib):
+    g = _golden()
+    mask = _mask_from_bits(g["op16_mask_bits"], 16)
+    with problem(mask.shape) as p:
+        p.set_geometry(mask)
+        y = p.operator_apply(g["op16_x"])
+        b = p.build_rhs((0.0, 1.0, 0.0))
+        avg, _ = p.recover((1.0, 0.0, 0.0), 0.1 * g["op16_x"])
+    assert rel_err(y, g["op16_y"]) < 1e-12
+    assert rel_err(b, g["op16_rhs_y"]) < 1e-12
+    assert rel_err(avg, g["op16_recover_avg"]) < 1e-12
+
+
+def test_golden_green_3x5x6_direct(gpu_lib):
+    g = _golden()
+    full = g["green_3x5x6"]  # (6, nz, ny, nx) from the reference, unsymmetrised
+    nz, ny, nx = full.shape[1:]
+    neg = full[:, (-np.arange(nz)) % nz][:, :, (-np.arange(ny)) % ny][:, :, :, (-np.arange(nx)) % nx]
+    want = 0.5 * (full + neg)[:, :, :, : nx // 2 + 1]
+    with problem((nz, ny, nx)) as p:
+        got = p.green_tensor()
+    assert rel_err(got, want) < 1e-13
