@@ -449,7 +449,9 @@ int fp::create_handle(int nx, int ny, int nz, double voxel_size, double mu, int 
     P.n = (long long)nx * ny * nz;
     P.nxh = nx / 2 + 1;
     P.nrows = (long long)ny * nz;
-    P.rs = (P.nxh + 1) & ~1LL;
+    // a multiple of 4 elements: every FP32 Green row and FP32/FP64 spectral
+    // row starts 16-byte aligned (TMA tensor maps need 16-byte strides)
+    P.rs = (P.nxh + 3) & ~3LL;
     P.nh = P.rs * P.nrows;
     P.h = voxel_size;
     P.mu = mu;
@@ -710,6 +712,9 @@ int fp_operator_apply(fp_handle h, const double* x, double* y) {
 int fp_operator_apply_device(fp_handle h, const double* d_x, double* d_y) {
     if (!h || !d_x || !d_y) return FP_ERR_INVALID;
     Problem& P = h->P;
+    // the vector kernels read two voxels (three double2) per thread
+    if ((reinterpret_cast<uintptr_t>(d_x) | reinterpret_cast<uintptr_t>(d_y)) & 15)
+        return fail(P, FP_ERR_INVALID, "VariationalOperator::apply: device vectors must be 16-byte aligned");
     int rc = need_geometry(P, "VariationalOperator::apply");
     if (rc) return rc;
     return device_operator_apply(P, d_x, d_y);

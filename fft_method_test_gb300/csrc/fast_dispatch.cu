@@ -10,7 +10,7 @@ namespace fp {
 
 bool fast_apply_supported(const Problem& P, int precision, int src_kind, int dst_kind, int stage) {
     (void)precision;
-    if (P.fast_off) return false;
+    if (P.fast_off || P.tma_off || !P.d_err) return false;
     if (src_kind != kSrcCompact || dst_kind != kDstCompact || stage != kStageFull) return false;
     return fast::edge_supported(P.nx) && fast::edge_supported(P.ny) && fast::edge_supported(P.nz);
 }
@@ -46,6 +46,7 @@ static cudaError_t fast_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     a.scale = 1.0 / (double)P.n;
     a.partials = P.d_partials;
     a.skip = aa.skip;
+    a.err = P.d_err;
 
     // x passes: tiles of `rows` grid rows, persistent over the tiles
     int rows = fast::x_rows_for(P.nx);
@@ -54,8 +55,13 @@ static cudaError_t fast_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     a.ntiles = (P.nrows + rows - 1) / rows;
     const int xthreads = ((3 * rows / 2 * fast::x_tpl(P.nx) + 31) / 32) * 32;
     const size_t xsmem = (size_t)(3 * rows / 2) * fast::x_ld_rt<T>(P.nx) * sizeof(T2);
+    // inverse x: two stages, each the raw half-spectrum rows of a tile or,
+    // after stage A, its padded lines
+    const size_t raw = (size_t)3 * rows * P.rs * sizeof(T2);
+    const int stage_bytes = (int)((std::max(raw, xsmem) + 15) & ~size_t(15));
+    const size_t xismem = 2 * (size_t)stage_bytes;
     const int fwd_per_sm = fast::x_blocks_per_sm<T>(P.nx, false, xthreads, xsmem);
-    const int inv_per_sm = fast::x_blocks_per_sm<T>(P.nx, true, xthreads, xsmem);
+    const int inv_per_sm = fast::x_blocks_per_sm<T>(P.nx, true, xthreads, xismem);
     const int xgrid_f = (int)std::min<long long>(a.ntiles, (long long)fwd_per_sm * P.sm_count);
     int xgrid_i = (int)std::min<long long>(a.ntiles, (long long)inv_per_sm * P.sm_count);
     xgrid_i = std::min(xgrid_i, kMaxPartials);
@@ -64,17 +70,21 @@ static cudaError_t fast_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     constexpr int TX = fast::col_tx<T>();
     const int ntx = (P.nxh + TX - 1) / TX;
     const dim3 ygrid(ntx, P.nz, 3);
-    const dim3 zgrid(ntx, P.ny, 1);
-    const size_t zsmem = (size_t)3 * TX * fast::col_ld_rt<T>(P.nz) * sizeof(T2) +
-                         (size_t)6 * P.nz * TX * sizeof(T);
+    // z pass: persistent, one CTA per SM (two pipeline stages of about 100 KB)
+    const dim3 zgrid((unsigned)std::min<long long>((long long)ntx * P.ny, P.sm_count), 1, 1);
+    const size_t zsmem = fast::z_smem_rt<T>(P.nz);
 
     cudaStream_t st = P.stream;
     cudaError_t e;
     if ((e = fast::run_xfwd<T>(P.nx, a, xgrid_f, xthreads, xsmem, st)) != cudaSuccess) return e;
     if ((e = fast::run_y<T>(P.ny, -1, a, ygrid, st)) != cudaSuccess) return e;
-    if ((e = fast::run_z<T>(P.nz, a, zgrid, zsmem, st)) != cudaSuccess) return e;
+    const CUtensorMap* smap = nullptr;
+    const CUtensorMap* gmap = nullptr;
+    if (!fast_z_maps(P, sizeof(T) == 8, TX, &smap, &gmap)) return cudaErrorNotSupported;
+    if ((e = fast::run_z<T>(P.nz, *smap, *gmap, a, zgrid, zsmem, st)) != cudaSuccess) return e;
     if ((e = fast::run_y<T>(P.ny, +1, a, ygrid, st)) != cudaSuccess) return e;
-    if ((e = fast::run_xinv<T>(P.nx, a, xgrid_i, xthreads, xsmem, st)) != cudaSuccess) return e;
+    if ((e = fast::run_xinv<T>(P.nx, a, stage_bytes, xgrid_i, xthreads, xismem, st)) != cudaSuccess)
+        return e;
     *nparts = xgrid_i;
     return cudaSuccess;
 }

@@ -27,8 +27,9 @@ cudaError_t run_xfwd(int n, const FastArgs& a, int grid, int threads, size_t sme
 }
 
 template <typename T>
-cudaError_t run_xinv(int n, const FastArgs& a, int grid, int threads, size_t smem, cudaStream_t s) {
-#define FP_CALL(N) FP_RUN((k_fx_inv<T, N>), grid, threads, smem, s, a)
+cudaError_t run_xinv(int n, const FastArgs& a, int stage_bytes, int grid, int threads, size_t smem,
+                     cudaStream_t s) {
+#define FP_CALL(N) FP_RUN((k_fx_inv<T, N>), grid, threads, smem, s, a, stage_bytes)
     FP_FAST_SWITCH(n, FP_CALL)
 #undef FP_CALL
     return cudaGetLastError();
@@ -48,9 +49,10 @@ cudaError_t run_y(int n, int dir, const FastArgs& a, dim3 grid, cudaStream_t s) 
 }
 
 template <typename T>
-cudaError_t run_z(int n, const FastArgs& a, dim3 grid, size_t smem, cudaStream_t s) {
+cudaError_t run_z(int n, const CUtensorMap& spec_map, const CUtensorMap& green_map, const FastArgs& a,
+                  dim3 grid, size_t smem, cudaStream_t s) {
     constexpr int TX = col_tx<T>();
-#define FP_CALL(N) FP_RUN((k_fz<T, N, TX>), grid, 3 * TX * Split<N>::R2, smem, s, a)
+#define FP_CALL(N) FP_RUN((k_fz<T, N, TX>), grid, 3 * TX * Split<N>::R2, smem, s, spec_map, green_map, a)
     FP_FAST_SWITCH(n, FP_CALL)
 #undef FP_CALL
     return cudaGetLastError();
@@ -83,9 +85,10 @@ int x_blocks_per_sm(int n, bool inverse, int threads, size_t smem) {
 
 #define FP_FAST_INSTANTIATE(T)                                                                      \
     template cudaError_t run_xfwd<T>(int, const FastArgs&, int, int, size_t, cudaStream_t);         \
-    template cudaError_t run_xinv<T>(int, const FastArgs&, int, int, size_t, cudaStream_t);         \
+    template cudaError_t run_xinv<T>(int, const FastArgs&, int, int, int, size_t, cudaStream_t);    \
     template cudaError_t run_y<T>(int, int, const FastArgs&, dim3, cudaStream_t);                   \
-    template cudaError_t run_z<T>(int, const FastArgs&, dim3, size_t, cudaStream_t);                \
+    template cudaError_t run_z<T>(int, const CUtensorMap&, const CUtensorMap&, const FastArgs&, dim3, \
+                                  size_t, cudaStream_t);                                            \
     template int x_blocks_per_sm<T>(int, bool, int, size_t);
 
 }  // namespace fast

@@ -23,10 +23,14 @@
 //              x-lines, two real lines per complex FFT, half spectrum out
 //   k_fcol     y pass, one component per CTA slice, TX kx columns per CTA
 //   k_fz       z pass: forward, 3x3 Green multiply, inverse, all three
-//              components in one CTA; the Green tile is prefetched into
-//              shared memory with cp.async while the forward transform runs
+//              components in one CTA; persistent CTAs with a two-stage TMA
+//              pipeline (cp.async.bulk.tensor boxes of the spectral and Green
+//              tiles of the next (kx, ky) tile load while the current one is
+//              transformed)
 //   k_fx_inv   C2R x lines, gather to the support, 1/N scale, per-CTA partial
-//              sums (component sums and the dot with a given vector)
+//              sums (component sums and the dot with a given vector);
+//              persistent CTAs, the next tile's half-spectrum rows arriving
+//              by cp.async while the current tile is transformed
 //
 // Shared-memory line strides are chosen so that the half-warp (FP32) or
 // quarter-warp (FP64) of every exchange touches distinct banks.
@@ -37,6 +41,7 @@
 #include "common.cuh"
 #include "fft_engine.cuh"
 #include "internal.h"
+#include "tma.cuh"
 
 namespace fp {
 namespace fast {
@@ -179,6 +184,7 @@ struct FastArgs {
     const double2* tw64z;
     void* spec;
     const void* green;
+    int* err;  // z pass: a bounded TMA wait gave up
     // x passes
     int rows;       // grid rows per tile (even)
     long long ntiles;
@@ -210,6 +216,20 @@ __device__ __forceinline__ const double2* tw_of<double>(const FastArgs& a, int a
 template <int N>
 __host__ __device__ constexpr int x_threads(int rows) {
     return ((3 * rows / 2 * Split<N>::R2 + 31) / 32) * 32;
+}
+
+// ---- cp.async (global -> shared, completion by group) ---------------------------
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                     static_cast<uint32_t>(__cvta_generic_to_shared(smem))),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory");
 }
 
 // ---- P1: scatter + R2C x -------------------------------------------------------
@@ -297,16 +317,23 @@ __global__ void __launch_bounds__(384) k_fx_fwd(FastArgs a) {
 
 // ---- P5: C2R x + gather + partial sums -------------------------------------------
 
+// Persistent CTAs walk tiles of `rows` grid rows.  The three component blocks
+// of a tile are contiguous rows of the half spectrum; cp.async brings the next
+// tile's rows into the other of two shared-memory stages while the current
+// tile is transformed.  Stage A of the inverse transform builds the complex
+// lines Z = A + iB of two real lines straight from the raw Hermitian half
+// spectra ([comp][row][rs], as copied); after a barrier the padded lines
+// overwrite the same stage.  stage_bytes covers the larger of the two layouts.
 template <typename T, int N>
-__global__ void __launch_bounds__(384) k_fx_inv(FastArgs a) {
+__global__ void __launch_bounds__(384) k_fx_inv(FastArgs a, int stage_bytes) {
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
     constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = R2;
     constexpr int LD = x_ld<N, T>();
     constexpr int NH = N / 2 + 1;
+    constexpr int SPC = 16 / sizeof(T2);  // elements per 16-byte copy
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double red[4 * 32];
-    T2* lines = reinterpret_cast<T2*>(smem_raw);
     const int RB = a.rows;
     const int tid = threadIdx.x;
     const int nthr = blockDim.x;
@@ -315,44 +342,74 @@ __global__ void __launch_bounds__(384) k_fx_inv(FastArgs a) {
     const T2* tw = tw_of<T>(a, 0);
     const T2* spec = reinterpret_cast<const T2*>(a.spec);
     const T scale = (T)a.scale;
+    const long long rs = a.rs;
     T acc[4] = {(T)0, (T)0, (T)0, (T)0};
-    for (long long tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+
+    auto issue = [&](long long tile, int st) {
+        T2* raw = reinterpret_cast<T2*>(smem_raw + st * (size_t)stage_bytes);
+        const long long r0 = tile * RB;
+        const int rows = (int)min((long long)RB, a.nrows - r0);
+        const int per_comp = (int)(rows * rs / SPC);  // rs is a multiple of 4: whole copies
+        for (int i = tid; i < 3 * per_comp; i += nthr) {
+            const int cc = i / per_comp;
+            const int j = i - cc * per_comp;
+            cp_async16(raw + (size_t)cc * RB * rs + (size_t)j * SPC,
+                       spec + cc * a.nh + r0 * rs + (long long)j * SPC);
+        }
+        cp_async_commit();
+    };
+
+    long long tile = blockIdx.x;
+    if (tile < a.ntiles) issue(tile, 0);
+    for (int it = 0; tile < a.ntiles; tile += gridDim.x, ++it) {
+        const int st = it & 1;
+        const long long next = tile + gridDim.x;
+        if (next < a.ntiles) {
+            issue(next, st ^ 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const T2* raw = reinterpret_cast<const T2*>(smem_raw + st * (size_t)stage_bytes);
+        T2* lines = reinterpret_cast<T2*>(smem_raw + st * (size_t)stage_bytes);
         const long long r0 = tile * RB;
         const int rows = (int)min((long long)RB, a.nrows - r0);
         const int nreal = 3 * rows;
         const int nqa = (nreal + 1) / 2;
-        // 1) complex lines Z = A + iB from the two Hermitian half spectra
-        for (int it = tid; it < nqa * NH; it += nthr) {
-            const int qq = it / NH;
-            const int k = it - qq * NH;
-            const int La = 2 * qq, rla = La / 3, ca = La - 3 * rla;
-            T2 A = spec[ca * a.nh + (r0 + rla) * a.rs + k];
-            T2 B = T2{};
-            const int Lb = La + 1;
-            if (Lb < nreal) {
-                const int rlb = Lb / 3, cb = Lb - 3 * rlb;
-                B = spec[cb * a.nh + (r0 + rlb) * a.rs + k];
-            }
-            if (k == 0 || (N % 2 == 0 && 2 * k == N)) {  // DC and Nyquist are real
-                A.y = (T)0;
-                B.y = (T)0;
-            }
-            lines[qq * LD + k] = cmk<T2>(A.x - B.y, A.y + B.x);
-            if (k > 0 && N - k >= NH) lines[qq * LD + (N - k)] = cmk<T2>(A.x + B.y, B.x - A.y);
-        }
-        __syncthreads();
-        // 2) inverse FFT (radices swapped: R2 first), result in natural order
         const bool act = q < nqa;
         T2* my = lines + (act ? q : 0) * LD;
         {
-            auto ld_nat = [&](int pos) { return my[pos]; };
-            stage_a<R2, R1, +1, TPL, true>(my, t, act, tw, ld_nat);
-            __syncthreads();
+            // complex line q carries real lines 2q (A) and 2q + 1 (B)
+            const int La = 2 * q, rla = La / 3, ca = La - 3 * rla;
+            const int Lb = La + 1, rlb = Lb / 3, cb = Lb - 3 * rlb;
+            const T2* ra = raw + ((size_t)ca * RB + rla) * rs;
+            const T2* rb = raw + ((size_t)cb * RB + rlb) * rs;
+            const bool hasb = Lb < nreal;
+            auto ld_herm = [&](int k) {
+                const bool lo = k < NH;
+                const int kk = lo ? k : N - k;
+                T2 A = ra[kk];
+                T2 B = hasb ? rb[kk] : T2{};
+                if (kk == 0 || 2 * kk == N) {  // DC and Nyquist are real
+                    A.y = (T)0;
+                    B.y = (T)0;
+                }
+                if (!lo) {  // Z[k] = conj(A[N-k]) + i conj(B[N-k])
+                    A.y = -A.y;
+                    B.y = -B.y;
+                }
+                return cmk<T2>(A.x - B.y, A.y + B.x);
+            };
+            stage_a<R2, R1, +1, TPL, true>(my, t, act, tw, ld_herm);
+        }
+        __syncthreads();
+        {
             auto st_nat = [&](int pos, T2 v) { my[pos] = v; };
             stage_b<R2, R1, +1, TPL, true>(my, t, act, st_nat);
         }
         __syncthreads();
-        // 3) gather to the support with the 1/N scale, partial sums
+        // gather to the support with the 1/N scale, partial sums
         {
             const int s0 = a.row_ptr[r0];
             const int s1 = a.row_ptr[r0 + rows];
@@ -372,7 +429,7 @@ __global__ void __launch_bounds__(384) k_fx_inv(FastArgs a) {
                 }
             }
         }
-        __syncthreads();
+        __syncthreads();  // this stage is refilled by the issue of iteration it + 1
     }
     double accd[4] = {(double)acc[0], (double)acc[1], (double)acc[2], (double)acc[3]};
     double out[4];
@@ -417,95 +474,120 @@ __global__ void __launch_bounds__(TX * Split<N>::R2) k_fcol_y(FastArgs a) {
 
 // ---- P3: z forward + Green + z inverse -------------------------------------------
 
-// cp.async of 8 bytes global -> shared (the FP32 Green rows are 8-byte aligned)
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(
-                     static_cast<uint32_t>(__cvta_generic_to_shared(smem))),
-                 "l"(gmem)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-
-// One CTA: TX kx columns of one ky row, all three components
-// (thread = column + TX * (owner + TPL * comp)).
+// Shared memory of one pipeline stage of the z pass: the spectral tile
+// (first raw [comp][kz][TX] as the TMA box lands, then the padded lines
+// [comp][TX][LD]) and the Green tile [6][kz][TX], each 128-byte aligned.
 template <typename T, int N, int TX>
-__global__ void __launch_bounds__(3 * TX * Split<N>::R2, 2) k_fz(FastArgs a) {
+__host__ __device__ constexpr size_t z_green_offset() {
+    return (((size_t)3 * TX * col_ld<N, T>() * 2 * sizeof(T)) + 127) & ~size_t(127);
+}
+template <typename T, int N, int TX>
+__host__ __device__ constexpr size_t z_stage_bytes() {
+    return (z_green_offset<T, N, TX>() + (size_t)6 * N * TX * sizeof(T) + 127) & ~size_t(127);
+}
+
+// Persistent CTAs walk the (kx tile, ky) tiles; thread = column + TX *
+// (owner + TPL * comp).  Two pipeline stages: while tile i is transformed,
+// one thread has the TMA engine bring the spectral tile (three boxes of
+// {2 TX reals, 1, nz}) and the Green tile (six boxes of {TX, 1, nz}) of tile
+// i + 1 into the other stage, completing on that stage's mbarrier.  Boxes
+// past the last kx column read zeros.  Waits are bounded: on a timeout the
+// CTA raises a.err and returns.
+template <typename T, int N, int TX>
+__global__ void __launch_bounds__(3 * TX * Split<N>::R2, 1)
+    k_fz(const __grid_constant__ CUtensorMap spec_map, const __grid_constant__ CUtensorMap green_map,
+         FastArgs a) {
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
     constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = R2;
     constexpr int LD = col_ld<N, T>();
-    constexpr int NT = 3 * TX * TPL;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T2* lines = reinterpret_cast<T2*>(smem_raw);          // [3][TX][LD]
-    T* gsm = reinterpret_cast<T*>(lines + 3 * TX * LD);   // [6][N][TX]
+    constexpr size_t STAGE = z_stage_bytes<T, N, TX>();
+    constexpr size_t GOFF = z_green_offset<T, N, TX>();
+    constexpr uint32_t TILE_BYTES = (uint32_t)(3 * N * TX * sizeof(T2) + 6 * N * TX * sizeof(T));
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
+    unsigned char* stage0 = smem_raw + 128;
     const int c = threadIdx.x % TX;
     const int t = (threadIdx.x / TX) % TPL;
     const int comp = threadIdx.x / (TX * TPL);
-    const int k0 = blockIdx.x * TX;
-    const bool act = k0 + c < a.nxh;
-    const long long ky = blockIdx.y;
+    const int ntx = (a.nxh + TX - 1) / TX;
+    const long long ntiles = (long long)ntx * a.ny;
     const T2* tw = tw_of<T>(a, 2);
-    // Green tile prefetch: 6 components x N kz rows x TX columns
-    {
-        const T* g = reinterpret_cast<const T*>(a.green);
-        constexpr int PER = 8 / sizeof(T);  // elements per 8-byte copy
-        constexpr int CPR = TX / PER;       // copies per row
-        const int ncols = min(TX, a.nxh - k0);
-        for (int i = threadIdx.x; i < 6 * N * CPR; i += NT) {
-            const int part = i % CPR;
-            const int row = i / CPR;  // gc * N + kz
-            const int gc = row / N;
-            const int kz = row - gc * N;
-            T* dstp = gsm + (size_t)row * TX + part * PER;
-            if (part * PER < ncols) {
-                const T* srcp = g + gc * a.nh + kz * a.plane + ky * a.rs + k0 + part * PER;
-                if (part * PER + PER <= ncols || sizeof(T) == 8) {
-                    cp_async8(dstp, srcp);
-                } else {
-                    dstp[0] = srcp[0];  // the last column of an odd-width row
-                }
-            }
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    auto issue = [&](long long tile, int st) {
+        unsigned char* base = stage0 + st * STAGE;
+        const int k0 = (int)(tile % ntx) * TX;
+        const int ky = (int)(tile / ntx);
+        mbar_arrive_expect_tx(&bars[st], TILE_BYTES);
+        for (int cc = 0; cc < 3; ++cc)
+            tma_load_4d(base + (size_t)cc * N * TX * sizeof(T2), &spec_map, 2 * k0, ky, 0, cc,
+                        &bars[st]);
+        for (int gc = 0; gc < 6; ++gc)
+            tma_load_4d(base + GOFF + (size_t)gc * N * TX * sizeof(T), &green_map, k0, ky, 0, gc,
+                        &bars[st]);
+    };
+
+    long long tile = blockIdx.x;
+    if (threadIdx.x == 0 && tile < ntiles) issue(tile, 0);
+    for (int i = 0; tile < ntiles; tile += gridDim.x, ++i) {
+        const int st = i & 1;
+        const long long next = tile + gridDim.x;
+        if (threadIdx.x == 0 && next < ntiles) {
+            fence_proxy_async_smem();
+            issue(next, st ^ 1);
         }
-        cp_async_commit();
-    }
-    T2* base = reinterpret_cast<T2*>(a.spec) + comp * a.nh + ky * a.rs + k0 + (act ? c : 0);
-    const long long es = a.plane;
-    T2* my = lines + (comp * TX + c) * LD;
-    // forward stage A from HBM, stage B back to the lines in natural order
-    {
-        auto ld_g = [&](int pos) { return base[pos * es]; };
-        stage_a<R1, R2, -1, TPL, false>(my, t, act, tw, ld_g);
-    }
-    __syncthreads();
-    {
-        auto st_nat = [&](int pos, T2 v) { my[pos] = v; };
-        stage_b<R1, R2, -1, TPL, true>(my, t, act, st_nat);
-    }
-    cp_async_wait_all();
-    __syncthreads();
-    // Green multiply while loading the inverse stage A (owner k1 = same owner)
-    {
-        const T2* lx = lines + (0 * TX + c) * LD;
-        const T2* ly = lines + (1 * TX + c) * LD;
-        const T2* lz = lines + (2 * TX + c) * LD;
-        // Green components of row `comp` of the symmetric tensor (xx xy xz yy yz zz)
-        const int g0 = comp == 0 ? 0 : (comp == 1 ? 1 : 2);
-        const int g1 = comp == 0 ? 1 : (comp == 1 ? 3 : 4);
-        const int g2 = comp == 0 ? 2 : (comp == 1 ? 4 : 5);
-        auto ld_green = [&](int pos) {
-            const T2 X = lx[pos], Y = ly[pos], Z = lz[pos];
-            const T a0 = gsm[((size_t)g0 * N + pos) * TX + c];
-            const T a1 = gsm[((size_t)g1 * N + pos) * TX + c];
-            const T a2 = gsm[((size_t)g2 * N + pos) * TX + c];
-            return cmk<T2>(a0 * X.x + a1 * Y.x + a2 * Z.x, a0 * X.y + a1 * Y.y + a2 * Z.y);
-        };
-        stage_a<R2, R1, +1, TPL, true>(my, t, act, tw, ld_green);
-    }
-    __syncthreads();
-    {
-        auto st_g = [&](int pos, T2 v) { base[pos * es] = v; };
-        stage_b<R2, R1, +1, TPL, false>(my, t, act, st_g);
+        if (!tma_pipeline_wait<T2>(bars, i, st, next < ntiles, a.err)) return;
+        T2* raw = reinterpret_cast<T2*>(stage0 + st * STAGE);
+        const T* gsm = reinterpret_cast<const T*>(stage0 + st * STAGE + GOFF);
+        const int k0 = (int)(tile % ntx) * TX;
+        const long long ky = tile / ntx;
+        const bool act = k0 + c < a.nxh;
+        T2* lines = raw;  // the padded lines reuse the raw tile's space
+        T2* my = lines + (comp * TX + c) * LD;
+        // forward stage A from the raw tile; Y into the lines after a barrier
+        {
+            const T2* rc = raw + (size_t)comp * N * TX + c;
+            auto ld_raw = [&](int pos) { return rc[pos * TX]; };
+            stage_a<R1, R2, -1, TPL, true>(my, t, act, tw, ld_raw);
+        }
+        __syncthreads();
+        {
+            auto st_nat = [&](int pos, T2 v) { my[pos] = v; };
+            stage_b<R1, R2, -1, TPL, true>(my, t, act, st_nat);
+        }
+        __syncthreads();
+        // Green multiply while loading the inverse stage A (owner k1 = same owner)
+        {
+            const T2* lx = lines + (0 * TX + c) * LD;
+            const T2* ly = lines + (1 * TX + c) * LD;
+            const T2* lz = lines + (2 * TX + c) * LD;
+            // row `comp` of the symmetric tensor (xx xy xz yy yz zz)
+            const int g0 = comp == 0 ? 0 : (comp == 1 ? 1 : 2);
+            const int g1 = comp == 0 ? 1 : (comp == 1 ? 3 : 4);
+            const int g2 = comp == 0 ? 2 : (comp == 1 ? 4 : 5);
+            auto ld_green = [&](int pos) {
+                const T2 X = lx[pos], Y = ly[pos], Z = lz[pos];
+                const T a0 = gsm[((size_t)g0 * N + pos) * TX + c];
+                const T a1 = gsm[((size_t)g1 * N + pos) * TX + c];
+                const T a2 = gsm[((size_t)g2 * N + pos) * TX + c];
+                return cmk<T2>(a0 * X.x + a1 * Y.x + a2 * Z.x, a0 * X.y + a1 * Y.y + a2 * Z.y);
+            };
+            stage_a<R2, R1, +1, TPL, true>(my, t, act, tw, ld_green);
+        }
+        __syncthreads();
+        {
+            T2* base = reinterpret_cast<T2*>(a.spec) + comp * a.nh + ky * a.rs + k0 + (act ? c : 0);
+            const long long es = a.plane;
+            auto st_g = [&](int pos, T2 v) { base[pos * es] = v; };
+            stage_b<R2, R1, +1, TPL, false>(my, t, act, st_g);
+        }
+        __syncthreads();  // this stage is refilled by the issue of iteration i + 1
     }
 }
 
@@ -569,14 +651,28 @@ int col_ld_rt(int n) {
     }
 }
 
+// dynamic shared memory of the z pass: mbarriers + two pipeline stages
+template <typename T>
+size_t z_smem_rt(int n) {
+    constexpr int TX = col_tx<T>();
+    switch (n) {
+        case 32: return 128 + 2 * z_stage_bytes<T, 32, TX>();
+        case 64: return 128 + 2 * z_stage_bytes<T, 64, TX>();
+        case 128: return 128 + 2 * z_stage_bytes<T, 128, TX>();
+        default: return 128 + 2 * z_stage_bytes<T, 256, TX>();
+    }
+}
+
 template <typename T>
 cudaError_t run_xfwd(int n, const FastArgs& a, int grid, int threads, size_t smem, cudaStream_t s);
 template <typename T>
-cudaError_t run_xinv(int n, const FastArgs& a, int grid, int threads, size_t smem, cudaStream_t s);
+cudaError_t run_xinv(int n, const FastArgs& a, int stage_bytes, int grid, int threads, size_t smem,
+                     cudaStream_t s);
 template <typename T>
 cudaError_t run_y(int n, int dir, const FastArgs& a, dim3 grid, cudaStream_t s);
 template <typename T>
-cudaError_t run_z(int n, const FastArgs& a, dim3 grid, size_t smem, cudaStream_t s);
+cudaError_t run_z(int n, const CUtensorMap& spec_map, const CUtensorMap& green_map, const FastArgs& a,
+                  dim3 grid, size_t smem, cudaStream_t s);
 // blocks of the x kernels resident per SM at this shared-memory size
 template <typename T>
 int x_blocks_per_sm(int n, bool inverse, int threads, size_t smem);

@@ -449,19 +449,6 @@ struct RawIo {
     }
 };
 
-template <typename T2>
-__device__ __forceinline__ bool tma_pipeline_wait(uint64_t* bars, int i, int b, bool prefetched,
-                                                  int* err) {
-    const bool ok = mbar_wait_bounded(&bars[b], (uint32_t)((i >> 1) & 1));
-    if (__syncthreads_or(!ok)) {
-        if (threadIdx.x == 0) {
-            atomicExch(err, 1);
-            if (prefetched) mbar_wait_bounded(&bars[b ^ 1], (uint32_t)(((i + 1) >> 1) & 1));
-        }
-        return false;
-    }
-    return true;
-}
 
 template <typename T, int S>
 __global__ void __launch_bounds__(256) k_ypass_tma(const __grid_constant__ CUtensorMap map, YArgs a,

@@ -72,7 +72,7 @@ struct Problem {
     int nx = 0, ny = 0, nz = 0;
     long long n = 0;      // voxels
     int nxh = 0;          // nx/2 + 1
-    long long rs = 0;     // row stride of spectral fields and Green tables: nxh rounded up to even
+    long long rs = 0;     // row stride of spectral fields and Green tables: nxh rounded up to a multiple of 4
     long long nh = 0;     // half spectrum points stored: rs * ny * nz
     long long nrows = 0;  // ny * nz
     double h = 1.0, mu = 1.0;
@@ -133,6 +133,11 @@ struct Problem {
 
     // TMA-fed y and z passes: [precision 0 = FP64, 1 = FP32]
     TmaCache tma_y[2], tma_z[2];
+    // specialised z pass: tensor maps of the spectral field and the Green
+    // table [precision 0 = FP64, 1 = FP32], keyed by the table's address
+    CUtensorMap fz_spec_map[2], fz_green_map[2];
+    const void* fz_green_ptr[2] = {nullptr, nullptr};
+    bool fz_valid[2] = {false, false};
     // MINRES iteration chunks replayed as CUDA graphs (FFTPERM_NO_GRAPHS=1: off).
     // Captured pointers and kernels depend on the geometry, the precision and
     // the tiling: every change of those releases the graphs.
@@ -175,6 +180,12 @@ bool fill_plan_radices(int n, FftPlanDev& d);
 cudaError_t launch_support(Problem& P);
 // Computes the Green table into g64 and/or g32 (either may be null).
 cudaError_t launch_green(Problem& P, double* g64, float* g32);
+
+// Tensor maps of the specialised z pass (kernels_fft.cu): the spectral field
+// as [3][nz][ny][2*nxh] reals with boxes {2*tx, 1, nz, 1} and the Green table
+// as [6][nz][ny][nxh] with boxes {tx, 1, nz, 1}.  false when TMA is
+// unavailable or the layout does not qualify.
+bool fast_z_maps(Problem& P, bool dbl, int tx, const CUtensorMap** spec, const CUtensorMap** green);
 
 // ---- operator passes (kernels_fft.cu) ----
 // Source of the forward x pass.

@@ -203,6 +203,41 @@ static bool tma_setup(Problem& P, bool dbl, int axis, int tpl, int padsh, TmaTil
     return true;
 }
 
+bool fast_z_maps(Problem& P, bool dbl, int tx, const CUtensorMap** spec, const CUtensorMap** green) {
+    if (!tma_encoder()) return false;
+    const int k = dbl ? 0 : 1;
+    const void* g = dbl ? (const void*)P.d_green64 : (const void*)P.d_green32;
+    if (!g || P.nz > 256) return false;
+    if (!P.fz_valid[k] || P.fz_green_ptr[k] != g) {
+        const size_t e = dbl ? sizeof(double) : sizeof(float);
+        const CUtensorMapDataType dt = dbl ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+        const cuuint32_t estr[4] = {1, 1, 1, 1};
+        // the spectral field: interleaved (re, im) reals
+        const cuuint64_t sd[4] = {(cuuint64_t)(2 * P.nxh), (cuuint64_t)P.ny, (cuuint64_t)P.nz, 3};
+        const cuuint64_t ss[3] = {(cuuint64_t)(2 * P.rs * e), (cuuint64_t)(2 * P.rs * P.ny * e),
+                                  (cuuint64_t)(2 * P.nh * e)};
+        const cuuint32_t sb[4] = {(cuuint32_t)(2 * tx), 1u, (cuuint32_t)P.nz, 1u};
+        CUresult r = tma_encoder()(&P.fz_spec_map[k], dt, 4, P.d_spec, sd, ss, sb, estr,
+                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return false;
+        // the Green table: six real blocks
+        const cuuint64_t gd[4] = {(cuuint64_t)P.nxh, (cuuint64_t)P.ny, (cuuint64_t)P.nz, 6};
+        const cuuint64_t gs[3] = {(cuuint64_t)(P.rs * e), (cuuint64_t)(P.rs * P.ny * e),
+                                  (cuuint64_t)(P.nh * e)};
+        const cuuint32_t gb[4] = {(cuuint32_t)tx, 1u, (cuuint32_t)P.nz, 1u};
+        r = tma_encoder()(&P.fz_green_map[k], dt, 4, const_cast<void*>(g), gd, gs, gb, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return false;
+        P.fz_green_ptr[k] = g;
+        P.fz_valid[k] = true;
+    }
+    *spec = &P.fz_spec_map[k];
+    *green = &P.fz_green_map[k];
+    return true;
+}
+
 static int choose_rows_per_cta(const Problem& P, int tpl, int ld, size_t elem) {
     int rows = 1;
     for (int r = 1; r <= 64; ++r) {

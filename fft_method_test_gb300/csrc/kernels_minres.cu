@@ -36,17 +36,31 @@ int vec_blocks(const Problem& P, long long m) {
     return (int)b;
 }
 
-// partial component sums (and optionally sum of squares) of an AoS vector
+// partial component sums and the sum of squares of an AoS vector (three
+// components per voxel).  Two voxels (three aligned double2) per thread keep
+// the component of every load static; the odd tail voxel goes to the first
+// thread of block 0.
 __global__ void k_sum3(const double* __restrict__ v, long long nb, double* partials) {
     __shared__ double red[4 * 32];
     double acc[4] = {0, 0, 0, 0};
-    const long long m = 3 * nb;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
-         i += (long long)gridDim.x * blockDim.x) {
-        const double x = v[i];
-        const int c = (int)(i % 3);
-        acc[c] += x;
-        acc[3] += x * x;
+    const long long npair = nb >> 1;
+    const double2* v2 = reinterpret_cast<const double2*>(v);
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < npair;
+         k += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int h = 0; h < 3; ++h) {
+            const double2 x = v2[3 * k + h];
+            acc[(2 * h) % 3] += x.x;
+            acc[(2 * h + 1) % 3] += x.y;
+            acc[3] += x.x * x.x + x.y * x.y;
+        }
+    }
+    if ((nb & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+        for (int c = 0; c < 3; ++c) {
+            const double x = v[3 * (nb - 1) + c];
+            acc[c] += x;
+            acc[3] += x * x;
+        }
     }
     double out[4];
     block_sum<4>(acc, red, out);
@@ -308,7 +322,7 @@ __global__ void k_zmean_from_partials(const double* __restrict__ partials, int n
 }  // namespace
 
 cudaError_t launch_sum3(Problem& P, const double* v, long long nb, double* out4) {
-    const int blocks = vec_blocks(P, 3 * nb);
+    const int blocks = vec_blocks(P, (nb + 1) / 2);
     FP_LAUNCHED(); k_sum3<<<blocks, kVecThreads, 0, P.stream>>>(v, nb, P.d_partials);
     FP_LAUNCHED(); k_reduce4<<<1, 256, 0, P.stream>>>(P.d_partials, blocks, out4);
     return cudaGetLastError();
@@ -513,17 +527,25 @@ namespace fp {
 
 namespace {
 
-// v = scale * (v - mean), mean = sums[c] * inv_nb (AoS components)
-__global__ void k_sub_mean(double* __restrict__ v, long long m, const double* __restrict__ sums,
+// v = scale * (v - mean), mean = sums[c] * inv_nb (AoS components; two
+// voxels per thread as in k_sum3)
+__global__ void k_sub_mean(double* __restrict__ v, long long nb, const double* __restrict__ sums,
                            double inv_nb, double scale) {
-    const double m0 = sums[0] * inv_nb, m1 = sums[1] * inv_nb, m2 = sums[2] * inv_nb;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % 3);
-        const double mz = c == 0 ? m0 : (c == 1 ? m1 : m2);
-        const double r = v[i] - mz;
-        v[i] = scale == 1.0 ? r : scale * r;
+    const double mz[3] = {sums[0] * inv_nb, sums[1] * inv_nb, sums[2] * inv_nb};
+    const long long npair = nb >> 1;
+    double2* v2 = reinterpret_cast<double2*>(v);
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < npair;
+         k += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int h = 0; h < 3; ++h) {
+            double2 x = v2[3 * k + h];
+            x.x = scale * (x.x - mz[(2 * h) % 3]);
+            x.y = scale * (x.y - mz[(2 * h + 1) % 3]);
+            v2[3 * k + h] = x;
+        }
     }
+    if ((nb & 1) && blockIdx.x == 0 && threadIdx.x == 0)
+        for (int c = 0; c < 3; ++c) v[3 * (nb - 1) + c] = scale * (v[3 * (nb - 1) + c] - mz[c]);
 }
 
 // sums over the support of a dense SoA field, per component
@@ -623,9 +645,8 @@ cudaError_t launch_axpby(Problem& P, double* out, double a, const double* x, dou
 }
 
 cudaError_t launch_sub_mean(Problem& P, double* v, const double* sums, double scale) {
-    const long long m = 3 * P.nb;
-    FP_LAUNCHED(); k_sub_mean<<<vec_blocks(P, m), kVecThreads, 0, P.stream>>>(
-        v, m, sums, P.nb > 0 ? 1.0 / (double)P.nb : 0.0, scale);
+    FP_LAUNCHED(); k_sub_mean<<<vec_blocks(P, (P.nb + 1) / 2), kVecThreads, 0, P.stream>>>(
+        v, P.nb, sums, P.nb > 0 ? 1.0 / (double)P.nb : 0.0, scale);
     return cudaGetLastError();
 }
 

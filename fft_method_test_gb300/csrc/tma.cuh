@@ -75,4 +75,22 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
         : "memory");
 }
 
+// Wait of a two-stage pipeline for stage b of iteration i (parity (i >> 1) & 1).
+// Every thread of the CTA calls it.  On a timeout the CTA raises *err, thread 0
+// waits (bounded) for its own prefetch of the other stage when one was issued,
+// and all threads get false and must return.
+template <typename T2>
+__device__ __forceinline__ bool tma_pipeline_wait(uint64_t* bars, int i, int b, bool prefetched,
+                                                  int* err) {
+    const bool ok = mbar_wait_bounded(&bars[b], (uint32_t)((i >> 1) & 1));
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) {
+            atomicExch(err, 1);
+            if (prefetched) mbar_wait_bounded(&bars[b ^ 1], (uint32_t)(((i + 1) >> 1) & 1));
+        }
+        return false;
+    }
+    return true;
+}
+
 }  // namespace fp

@@ -74,6 +74,11 @@ int fp_synchronize(fp_handle h);
  * (every handle, device and stream).  A diagnostic with no counterpart in the
  * reference: the difference across a region counts the kernels it queued. */
 long long fp_kernel_launch_count(void);
+/* A diagnostic with no counterpart in the reference: the FP64 FMA throughput
+ * of the current device in TFLOP/s (2 flops per FMA), measured with a kernel
+ * of independent FMA chains on the legacy default stream; *ms receives the
+ * time of one launch.  Either output may be NULL. */
+int fp_measure_fp64_rate(double* tflops, double* ms);
 /* Precision of later applies/solves (FP_PREC_*). */
 int fp_set_precision(fp_handle h, int precision);
 
@@ -108,7 +113,8 @@ int fp_background_force(fp_handle h, const double grad[3], double* f0_soa);
 /* VariationalOperator::apply, the ILinearOperator of the method
  * (src/bignonnet/VariationalOperator.cpp:19-41): y = A x, 3*N_B doubles. */
 int fp_operator_apply(fp_handle h, const double* x, double* y);
-/* The same with device pointers on the handle's stream (inputs resident in HBM). */
+/* The same with device pointers on the handle's stream (inputs resident in
+ * HBM), 16-byte aligned (FP_ERR_INVALID otherwise). */
 int fp_operator_apply_device(fp_handle h, const double* d_x, double* d_y);
 /* VariationalRHS::build (src/bignonnet/VariationalRHS.cpp:15-31). */
 int fp_build_rhs(fp_handle h, const double grad[3], double* b);

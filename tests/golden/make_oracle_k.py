@@ -20,7 +20,9 @@ Cases:
   c4_96_grf    batch cell seed 2027: 96^3 Gaussian field, porosity 0.493, tol 1e-10
   c4_160_sph   batch cell seed 2012: 160^3 spheres r 3-10, porosity 0.337, tol 1e-10
   c2_128_sph   the Brinkman cell (128^3 spheres r 8, porosity 0.45, seed 1002), tol 1e-10
-  grf256       the benchmark cell (256^3, l 6, porosity 0.35, seed 1003), tol 1e-8
+  grf256       the benchmark cell (256^3, l 6, porosity 0.35, seed 1003), tol 1e-7 (the
+               benchmark's own stopping tolerance: its iteration counts are the
+               CPU reference's at that tolerance)
 """
 from __future__ import annotations
 
@@ -47,7 +49,7 @@ CASES = {
     "c4_96_grf": (lambda: G.batch_cell(2027), 1e-10),
     "c4_160_sph": (lambda: G.batch_cell(2012), 1e-10),
     "c2_128_sph": (lambda: G.spheres(128, 8.0, 0.45, seed=1002), 1e-10),
-    "grf256": (lambda: G.gaussian_field(256, 6.0, 0.35, seed=1003), 1e-8),
+    "grf256": (lambda: G.gaussian_field(256, 6.0, 0.35, seed=1003), 1e-7),
 }
 
 

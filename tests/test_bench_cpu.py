@@ -49,16 +49,41 @@ def test_batch_workload_matches_its_specification():
         assert abs(m.mean() - phi) < 0.02, (i, m.mean(), phi)
 
 
-def test_cpu_baseline_extrapolation(restatement):
-    """The CPU baseline times the oracle's set-up and applies on the given
-    cell and extrapolates to 3 x (Green precompute + (iterations/3 + 2)
-    applies), the reference's per-load-case structure."""
+def test_cpu_model_units_and_prediction(restatement):
+    """The CPU baseline times the oracle's set-up, one apply and one MINRES
+    iteration on the cell; seconds to K = set-ups + per load case two applies
+    (RHS, recovery) + iterations x iteration time."""
     import bench
     from fft_method_test_gb300 import geometry as G
 
     mask = G.spheres(16, 3.0, 0.6, seed=7)
-    total, cores, info = bench.cpu_sample(mask, 300, threads=1, sample_applies=2)
-    assert cores == 1 and info["sample_applies"] == 2
-    expect = 3 * (info["setup_s"] + (300 / 3.0 + 2) * info["apply_s"])
-    assert abs(total - expect) <= 1e-12 * expect
-    assert info["setup_s"] > 0 and info["apply_s"] > 0
+    u = bench.cpu_units(mask, threads=1)
+    assert u["setup_s"] > 0 and u["apply_s"] > 0 and u["iter_s"] > 0
+    its = [100, 120, 80]
+    want = 3 * u["setup_s"] + sum(2 * u["apply_s"] + i * u["iter_s"] for i in its)
+    assert abs(bench.cpu_predict(u, its, setups=3) - want) <= 1e-12 * want
+
+
+def test_cpu_model_check_reports_a_full_solve(restatement):
+    import bench
+    from fft_method_test_gb300 import geometry as G
+
+    chk = bench.cpu_model_check(G.spheres(16, 3.0, 0.6, seed=7), 1e-6, threads=1)
+    assert chk["measured_s"] > 0 and chk["predicted_s"] > 0
+    assert len(chk["iterations"]) == 3 and all(i > 0 for i in chk["iterations"])
+    assert abs(chk["rel_err"]) < 1.0
+
+
+def test_oracle_fixture_requires_the_same_mask():
+    """The committed oracle K is used only for the very cell it was computed on."""
+    import bench
+
+    from fft_method_test_gb300 import geometry as G
+
+    m = G.gaussian_field(64, 6.0, 0.35, seed=3064)
+    fx = bench.oracle_fixture("grf64", m)
+    assert fx is not None and fx["K"].shape == (3, 3) and len(fx["iterations"]) == 3
+    m2 = m.copy()
+    m2.flat[0] ^= 1
+    assert bench.oracle_fixture("grf64", m2) is None
+    assert bench.oracle_fixture("no_such_cell", m) is None
