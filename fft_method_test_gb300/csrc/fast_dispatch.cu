@@ -49,7 +49,8 @@ static cudaError_t fast_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     a.err = P.d_err;
 
     // x passes: tiles of `rows` grid rows, persistent over the tiles
-    int rows = fast::x_rows_for(P.nx);
+    // grid rows per tile: the tuned cap when set (even), else about 192 threads
+    int rows = P.x_rows > 0 ? std::max(2, P.x_rows & ~1) : fast::x_rows_for(P.nx);
     if (rows > P.nrows) rows = (int)((P.nrows + 1) & ~1LL);
     a.rows = rows;
     a.ntiles = (P.nrows + rows - 1) / rows;

@@ -36,10 +36,12 @@ int vec_blocks(const Problem& P, long long m) {
     return (int)b;
 }
 
-// partial component sums and the sum of squares of an AoS vector (three
+// partial component sums (and with SQUARES the sum of squares; GB300's FP64
+// pipe is narrow, so the plain sums skip them) of an AoS vector (three
 // components per voxel).  Two voxels (three aligned double2) per thread keep
 // the component of every load static; the odd tail voxel goes to the first
 // thread of block 0.
+template <bool SQUARES>
 __global__ void k_sum3(const double* __restrict__ v, long long nb, double* partials) {
     __shared__ double red[4 * 32];
     double acc[4] = {0, 0, 0, 0};
@@ -52,7 +54,7 @@ __global__ void k_sum3(const double* __restrict__ v, long long nb, double* parti
             const double2 x = v2[3 * k + h];
             acc[(2 * h) % 3] += x.x;
             acc[(2 * h + 1) % 3] += x.y;
-            acc[3] += x.x * x.x + x.y * x.y;
+            if (SQUARES) acc[3] += x.x * x.x + x.y * x.y;
         }
     }
     if ((nb & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -323,7 +325,7 @@ __global__ void k_zmean_from_partials(const double* __restrict__ partials, int n
 
 cudaError_t launch_sum3(Problem& P, const double* v, long long nb, double* out4) {
     const int blocks = vec_blocks(P, (nb + 1) / 2);
-    FP_LAUNCHED(); k_sum3<<<blocks, kVecThreads, 0, P.stream>>>(v, nb, P.d_partials);
+    FP_LAUNCHED(); k_sum3<false><<<blocks, kVecThreads, 0, P.stream>>>(v, nb, P.d_partials);
     FP_LAUNCHED(); k_reduce4<<<1, 256, 0, P.stream>>>(P.d_partials, blocks, out4);
     return cudaGetLastError();
 }
@@ -349,7 +351,7 @@ cudaError_t minres_start(Problem& P, const double* b, const double* x0, double t
     if (e != cudaSuccess) return e;
     const int blocks = vec_blocks(P, m);
     // |b|
-    FP_LAUNCHED(); k_sum3<<<blocks, kVecThreads, 0, P.stream>>>(b, P.nb, P.d_partials);
+    FP_LAUNCHED(); k_sum3<true><<<blocks, kVecThreads, 0, P.stream>>>(b, P.nb, P.d_partials);
     FP_LAUNCHED(); k_start_norms<<<1, 256, 0, P.stream>>>(P.d_sc, P.d_partials, blocks, 0);
     // x = x0 or 0
     if (x0) {
@@ -374,7 +376,7 @@ cudaError_t minres_start(Problem& P, const double* b, const double* x0, double t
         FP_LAUNCHED(); k_residual0<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, b, P.d_z, nullptr, m, 0);
     }
     // beta1 = |r0|
-    FP_LAUNCHED(); k_sum3<<<blocks, kVecThreads, 0, P.stream>>>(P.d_z, P.nb, P.d_partials);
+    FP_LAUNCHED(); k_sum3<true><<<blocks, kVecThreads, 0, P.stream>>>(P.d_z, P.nb, P.d_partials);
     FP_LAUNCHED(); k_start_norms<<<1, 256, 0, P.stream>>>(P.d_sc, P.d_partials, blocks, 1);
     e = cudaMemcpyAsync(P.h_sc, P.d_sc, sizeof(MinresScalars), cudaMemcpyDeviceToHost, P.stream);
     if (e != cudaSuccess) return e;
@@ -417,7 +419,7 @@ cudaError_t minres_start(Problem& P, const double* b, const double* x0, double t
     cudaMemsetAsync(P.d_w[0], 0, sizeof(double) * m, P.stream);
     cudaMemsetAsync(P.d_w[1], 0, sizeof(double) * m, P.stream);
     // component sums of v (input mean of the first apply)
-    FP_LAUNCHED(); k_sum3<<<blocks, kVecThreads, 0, P.stream>>>(P.d_v[0], P.nb, P.d_partials);
+    FP_LAUNCHED(); k_sum3<false><<<blocks, kVecThreads, 0, P.stream>>>(P.d_v[0], P.nb, P.d_partials);
     FP_LAUNCHED(); k_reduce4<<<1, 256, 0, P.stream>>>(P.d_partials, blocks, P.d_red + 8);
     // copy the three sums into sc->vsum
     cudaMemcpyAsync(&P.d_sc->vsum[0], P.d_red + 8, sizeof(double) * 3, cudaMemcpyDeviceToDevice,
@@ -529,6 +531,7 @@ namespace {
 
 // v = scale * (v - mean), mean = sums[c] * inv_nb (AoS components; two
 // voxels per thread as in k_sum3)
+template <bool SCALE>
 __global__ void k_sub_mean(double* __restrict__ v, long long nb, const double* __restrict__ sums,
                            double inv_nb, double scale) {
     const double mz[3] = {sums[0] * inv_nb, sums[1] * inv_nb, sums[2] * inv_nb};
@@ -539,8 +542,12 @@ __global__ void k_sub_mean(double* __restrict__ v, long long nb, const double* _
 #pragma unroll
         for (int h = 0; h < 3; ++h) {
             double2 x = v2[3 * k + h];
-            x.x = scale * (x.x - mz[(2 * h) % 3]);
-            x.y = scale * (x.y - mz[(2 * h + 1) % 3]);
+            x.x = x.x - mz[(2 * h) % 3];
+            x.y = x.y - mz[(2 * h + 1) % 3];
+            if (SCALE) {
+                x.x *= scale;
+                x.y *= scale;
+            }
             v2[3 * k + h] = x;
         }
     }
@@ -645,8 +652,13 @@ cudaError_t launch_axpby(Problem& P, double* out, double a, const double* x, dou
 }
 
 cudaError_t launch_sub_mean(Problem& P, double* v, const double* sums, double scale) {
-    FP_LAUNCHED(); k_sub_mean<<<vec_blocks(P, (P.nb + 1) / 2), kVecThreads, 0, P.stream>>>(
-        v, P.nb, sums, P.nb > 0 ? 1.0 / (double)P.nb : 0.0, scale);
+    const int blocks = vec_blocks(P, (P.nb + 1) / 2);
+    const double inv_nb = P.nb > 0 ? 1.0 / (double)P.nb : 0.0;
+    FP_LAUNCHED();
+    if (scale == 1.0)
+        k_sub_mean<false><<<blocks, kVecThreads, 0, P.stream>>>(v, P.nb, sums, inv_nb, scale);
+    else
+        k_sub_mean<true><<<blocks, kVecThreads, 0, P.stream>>>(v, P.nb, sums, inv_nb, scale);
     return cudaGetLastError();
 }
 
