@@ -70,7 +70,14 @@ static cudaError_t fast_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     // column passes
     constexpr int TX = fast::col_tx<T>();
     const int ntx = (P.nxh + TX - 1) / TX;
-    const dim3 ygrid(ntx, P.nz, 3);
+    const CUtensorMap* smap = nullptr;
+    const CUtensorMap* gmap = nullptr;
+    const CUtensorMap* ymap = nullptr;
+    if (!fast_maps(P, sizeof(T) == 8, TX, &smap, &gmap, &ymap)) return cudaErrorNotSupported;
+    // y passes: persistent TMA-fed CTAs, as many as fit per SM
+    const size_t ysmem = fast::y_smem_rt<T>(P.ny);
+    const int ygrid = (int)std::min<long long>(
+        (long long)3 * ntx * P.nz, (long long)fast::y_blocks_per_sm<T>(P.ny, ysmem) * P.sm_count);
     // z pass: persistent, one CTA per SM (two pipeline stages of about 100 KB)
     const dim3 zgrid((unsigned)std::min<long long>((long long)ntx * P.ny, P.sm_count), 1, 1);
     const size_t zsmem = fast::z_smem_rt<T>(P.nz);
@@ -78,12 +85,9 @@ static cudaError_t fast_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     cudaStream_t st = P.stream;
     cudaError_t e;
     if ((e = fast::run_xfwd<T>(P.nx, a, xgrid_f, xthreads, xsmem, st)) != cudaSuccess) return e;
-    if ((e = fast::run_y<T>(P.ny, -1, a, ygrid, st)) != cudaSuccess) return e;
-    const CUtensorMap* smap = nullptr;
-    const CUtensorMap* gmap = nullptr;
-    if (!fast_z_maps(P, sizeof(T) == 8, TX, &smap, &gmap)) return cudaErrorNotSupported;
+    if ((e = fast::run_y_tma<T>(P.ny, -1, *ymap, a, ygrid, ysmem, st)) != cudaSuccess) return e;
     if ((e = fast::run_z<T>(P.nz, *smap, *gmap, a, zgrid, zsmem, st)) != cudaSuccess) return e;
-    if ((e = fast::run_y<T>(P.ny, +1, a, ygrid, st)) != cudaSuccess) return e;
+    if ((e = fast::run_y_tma<T>(P.ny, +1, *ymap, a, ygrid, ysmem, st)) != cudaSuccess) return e;
     if ((e = fast::run_xinv<T>(P.nx, a, stage_bytes, xgrid_i, xthreads, xismem, st)) != cudaSuccess)
         return e;
     *nparts = xgrid_i;

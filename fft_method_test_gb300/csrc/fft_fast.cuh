@@ -21,7 +21,9 @@
 // Passes (kernels below):
 //   k_fx_fwd   scatter of the compact vector (minus its mean) into real
 //              x-lines, two real lines per complex FFT, half spectrum out
-//   k_fcol     y pass, one component per CTA slice, TX kx columns per CTA
+//   k_fy       y pass, one component per tile of TX kx columns; persistent
+//              CTAs with a two-stage TMA pipeline (k_fcol_y: the same pass
+//              reading HBM directly, where TMA is off)
 //   k_fz       z pass: forward, 3x3 Green multiply, inverse, all three
 //              components in one CTA; persistent CTAs with a two-stage TMA
 //              pipeline (cp.async.bulk.tensor boxes of the spectral and Green
@@ -116,22 +118,37 @@ __host__ __device__ constexpr int x_ld() {
     return tpl < G ? base + tpl : base;
 }
 
+// ---- barriers -------------------------------------------------------------------
+
+// the whole CTA
+struct CtaBarrier {
+    __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+// the `count` threads (a multiple of 32) of one named barrier `id` (1..15)
+struct GroupBarrier {
+    int id, count;
+    __device__ __forceinline__ void operator()() const {
+        asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+    }
+};
+
 // ---- four-step stages --------------------------------------------------------
 
 // Stage A for owners a = t + TPL*j (j < RB/TPL): loads RA values through
 // load(pos) (pos = RB*i + a), DFT-RA, twiddle W_N^(S a k), stores Y[k][a] at
-// line[k*(RB+1) + a].  With SYNC the CTA synchronises between the loads and
-// the stores (the loads read the same lines).
-template <int RA, int RB, int S, int TPL, bool SYNC, typename T2, class Load>
+// line[k*(RB+1) + a].  With SYNC, bar() runs between the loads and the
+// stores (the loads read the same lines).
+template <int RA, int RB, int S, int TPL, bool SYNC, typename T2, class Load,
+          class Bar = CtaBarrier>
 __device__ __forceinline__ void stage_a(T2* line, int t, bool active, const T2* __restrict__ tw,
-                                        Load& load) {
+                                        Load& load, Bar bar = Bar{}) {
     constexpr int J = RB / TPL;
     T2 v[J][RA];
 #pragma unroll
     for (int j = 0; j < J; ++j)
 #pragma unroll
         for (int i = 0; i < RA; ++i) v[j][i] = active ? load(RB * i + t + TPL * j) : T2{};
-    if (SYNC) __syncthreads();
+    if (SYNC) bar();
     if (active) {
 #pragma unroll
         for (int j = 0; j < J; ++j) {
@@ -148,10 +165,12 @@ __device__ __forceinline__ void stage_a(T2* line, int t, bool active, const T2* 
 }
 
 // Stage B for owners k = t + TPL*j (j < RA/TPL): loads Y[k][a] (a < RB),
-// DFT-RB, hands X[k + RA*m] to store(pos, value).  With SYNC the CTA
-// synchronises between the loads and the stores.
-template <int RA, int RB, int S, int TPL, bool SYNC, typename T2, class Store>
-__device__ __forceinline__ void stage_b(const T2* line, int t, bool active, Store& store) {
+// DFT-RB, hands X[k + RA*m] to store(pos, value).  With SYNC, bar() runs
+// between the loads and the stores.
+template <int RA, int RB, int S, int TPL, bool SYNC, typename T2, class Store,
+          class Bar = CtaBarrier>
+__device__ __forceinline__ void stage_b(const T2* line, int t, bool active, Store& store,
+                                        Bar bar = Bar{}) {
     constexpr int J = RA / TPL;
     T2 u[J][RB];
 #pragma unroll
@@ -159,7 +178,7 @@ __device__ __forceinline__ void stage_b(const T2* line, int t, bool active, Stor
 #pragma unroll
         for (int a = 0; a < RB; ++a)
             u[j][a] = active ? line[(t + TPL * j) * (RB + 1) + a] : T2{};
-    if (SYNC) __syncthreads();
+    if (SYNC) bar();
     if (active) {
 #pragma unroll
         for (int j = 0; j < J; ++j) {
@@ -241,7 +260,7 @@ __global__ void __launch_bounds__(384) k_fx_fwd(FastArgs a) {
     constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = R2;
     constexpr int LD = x_ld<N, T>();
     constexpr int NH = N / 2 + 1;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     T2* lines = reinterpret_cast<T2*>(smem_raw);
     const int RB = a.rows;
     const int nq = 3 * RB / 2;
@@ -332,7 +351,7 @@ __global__ void __launch_bounds__(384) k_fx_inv(FastArgs a, int stage_bytes) {
     constexpr int LD = x_ld<N, T>();
     constexpr int NH = N / 2 + 1;
     constexpr int SPC = 16 / sizeof(T2);  // elements per 16-byte copy
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ double red[4 * 32];
     const int RB = a.rows;
     const int tid = threadIdx.x;
@@ -474,12 +493,20 @@ __global__ void __launch_bounds__(TX * Split<N>::R2) k_fcol_y(FastArgs a) {
 
 // ---- P3: z forward + Green + z inverse -------------------------------------------
 
-// Shared memory of one pipeline stage of the z pass: the spectral tile
-// (first raw [comp][kz][TX] as the TMA box lands, then the padded lines
-// [comp][TX][LD]) and the Green tile [6][kz][TX], each 128-byte aligned.
+// Component stride (elements) of the spectral tile in shared memory: the
+// padded lines of one component, rounded up so that each component block
+// starts 128-byte aligned (a TMA destination) and the blocks never overlap.
+template <typename T, int N, int TX>
+__host__ __device__ constexpr int comp_stride() {
+    return (int)(((size_t)TX * col_ld<N, T>() * 2 * sizeof(T) + 127) / 128 * 128 / (2 * sizeof(T)));
+}
+
+// Shared memory of one pipeline stage of the z pass: the spectral tile (per
+// component first raw [kz][TX] as the TMA box lands, then the padded lines
+// [TX][LD] in the same block) and the Green tile [6][kz][TX].
 template <typename T, int N, int TX>
 __host__ __device__ constexpr size_t z_green_offset() {
-    return (((size_t)3 * TX * col_ld<N, T>() * 2 * sizeof(T)) + 127) & ~size_t(127);
+    return (size_t)3 * comp_stride<T, N, TX>() * 2 * sizeof(T);
 }
 template <typename T, int N, int TX>
 __host__ __device__ constexpr size_t z_stage_bytes() {
@@ -491,8 +518,10 @@ __host__ __device__ constexpr size_t z_stage_bytes() {
 // one thread has the TMA engine bring the spectral tile (three boxes of
 // {2 TX reals, 1, nz}) and the Green tile (six boxes of {TX, 1, nz}) of tile
 // i + 1 into the other stage, completing on that stage's mbarrier.  Boxes
-// past the last kx column read zeros.  Waits are bounded: on a timeout the
-// CTA raises a.err and returns.
+// past the last kx column read zeros.  The phases that touch one component
+// only synchronise that component's threads (named barrier 1 + comp); the
+// Green multiply reads all three.  Waits are bounded: on a timeout the CTA
+// raises a.err and returns.
 template <typename T, int N, int TX>
 __global__ void __launch_bounds__(3 * TX * Split<N>::R2, 1)
     k_fz(const __grid_constant__ CUtensorMap spec_map, const __grid_constant__ CUtensorMap green_map,
@@ -501,6 +530,7 @@ __global__ void __launch_bounds__(3 * TX * Split<N>::R2, 1)
     using T2 = c_t<T>;
     constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = R2;
     constexpr int LD = col_ld<N, T>();
+    constexpr int CS = comp_stride<T, N, TX>();
     constexpr size_t STAGE = z_stage_bytes<T, N, TX>();
     constexpr size_t GOFF = z_green_offset<T, N, TX>();
     constexpr uint32_t TILE_BYTES = (uint32_t)(3 * N * TX * sizeof(T2) + 6 * N * TX * sizeof(T));
@@ -510,6 +540,7 @@ __global__ void __launch_bounds__(3 * TX * Split<N>::R2, 1)
     const int c = threadIdx.x % TX;
     const int t = (threadIdx.x / TX) % TPL;
     const int comp = threadIdx.x / (TX * TPL);
+    const GroupBarrier gbar{1 + comp, TX * TPL};
     const int ntx = (a.nxh + TX - 1) / TX;
     const long long ntiles = (long long)ntx * a.ny;
     const T2* tw = tw_of<T>(a, 2);
@@ -526,8 +557,7 @@ __global__ void __launch_bounds__(3 * TX * Split<N>::R2, 1)
         const int ky = (int)(tile / ntx);
         mbar_arrive_expect_tx(&bars[st], TILE_BYTES);
         for (int cc = 0; cc < 3; ++cc)
-            tma_load_4d(base + (size_t)cc * N * TX * sizeof(T2), &spec_map, 2 * k0, ky, 0, cc,
-                        &bars[st]);
+            tma_load_4d(base + (size_t)cc * CS * sizeof(T2), &spec_map, 2 * k0, ky, 0, cc, &bars[st]);
         for (int gc = 0; gc < 6; ++gc)
             tma_load_4d(base + GOFF + (size_t)gc * N * TX * sizeof(T), &green_map, k0, ky, 0, gc,
                         &bars[st]);
@@ -543,30 +573,29 @@ __global__ void __launch_bounds__(3 * TX * Split<N>::R2, 1)
             issue(next, st ^ 1);
         }
         if (!tma_pipeline_wait<T2>(bars, i, st, next < ntiles, a.err)) return;
-        T2* raw = reinterpret_cast<T2*>(stage0 + st * STAGE);
+        T2* blk = reinterpret_cast<T2*>(stage0 + st * STAGE);
         const T* gsm = reinterpret_cast<const T*>(stage0 + st * STAGE + GOFF);
         const int k0 = (int)(tile % ntx) * TX;
         const long long ky = tile / ntx;
         const bool act = k0 + c < a.nxh;
-        T2* lines = raw;  // the padded lines reuse the raw tile's space
-        T2* my = lines + (comp * TX + c) * LD;
-        // forward stage A from the raw tile; Y into the lines after a barrier
+        T2* my = blk + comp * CS + c * LD;  // padded line in this component's block
+        // forward stage A from the raw box; Y into the lines after the group barrier
         {
-            const T2* rc = raw + (size_t)comp * N * TX + c;
+            const T2* rc = blk + comp * CS + c;
             auto ld_raw = [&](int pos) { return rc[pos * TX]; };
-            stage_a<R1, R2, -1, TPL, true>(my, t, act, tw, ld_raw);
+            stage_a<R1, R2, -1, TPL, true>(my, t, act, tw, ld_raw, gbar);
         }
-        __syncthreads();
+        gbar();
         {
             auto st_nat = [&](int pos, T2 v) { my[pos] = v; };
-            stage_b<R1, R2, -1, TPL, true>(my, t, act, st_nat);
+            stage_b<R1, R2, -1, TPL, true>(my, t, act, st_nat, gbar);
         }
         __syncthreads();
         // Green multiply while loading the inverse stage A (owner k1 = same owner)
         {
-            const T2* lx = lines + (0 * TX + c) * LD;
-            const T2* ly = lines + (1 * TX + c) * LD;
-            const T2* lz = lines + (2 * TX + c) * LD;
+            const T2* lx = blk + 0 * CS + c * LD;
+            const T2* ly = blk + 1 * CS + c * LD;
+            const T2* lz = blk + 2 * CS + c * LD;
             // row `comp` of the symmetric tensor (xx xy xz yy yz zz)
             const int g0 = comp == 0 ? 0 : (comp == 1 ? 1 : 2);
             const int g1 = comp == 0 ? 1 : (comp == 1 ? 3 : 4);
@@ -578,13 +607,93 @@ __global__ void __launch_bounds__(3 * TX * Split<N>::R2, 1)
                 const T a2 = gsm[((size_t)g2 * N + pos) * TX + c];
                 return cmk<T2>(a0 * X.x + a1 * Y.x + a2 * Z.x, a0 * X.y + a1 * Y.y + a2 * Z.y);
             };
-            stage_a<R2, R1, +1, TPL, true>(my, t, act, tw, ld_green);
+            stage_a<R2, R1, +1, TPL, true>(my, t, act, tw, ld_green);  // CTA barrier
         }
-        __syncthreads();
+        gbar();
         {
             T2* base = reinterpret_cast<T2*>(a.spec) + comp * a.nh + ky * a.rs + k0 + (act ? c : 0);
             const long long es = a.plane;
             auto st_g = [&](int pos, T2 v) { base[pos * es] = v; };
+            stage_b<R2, R1, +1, TPL, false>(my, t, act, st_g);
+        }
+        __syncthreads();  // this stage is refilled by the issue of iteration i + 1
+    }
+}
+
+// ---- P2 / P4: y pass fed by TMA ------------------------------------------------
+
+// One pipeline stage of the y pass: the raw box [ny][TX] of one component,
+// overwritten in place by the padded lines [TX][LD].
+template <typename T, int N, int TX>
+__host__ __device__ constexpr size_t y_stage_bytes() {
+    return (size_t)comp_stride<T, N, TX>() * 2 * sizeof(T);
+}
+
+// Persistent CTAs walk the (kx tile, z plane, component) tiles; thread =
+// column + TX * owner.  While tile i is transformed, the TMA engine brings
+// the {2 TX reals, ny} box of tile i + 1 into the other stage.  The last
+// stage writes HBM directly.  Bounded waits as in k_fz.
+template <typename T, int N, int S, int TX>
+__global__ void __launch_bounds__(TX * Split<N>::R2)
+    k_fy(const __grid_constant__ CUtensorMap spec_map, FastArgs a) {
+    if (a.skip && *a.skip) return;
+    using T2 = c_t<T>;
+    constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = R2;
+    constexpr int LD = col_ld<N, T>();
+    constexpr size_t STAGE = y_stage_bytes<T, N, TX>();
+    constexpr uint32_t TILE_BYTES = (uint32_t)(N * TX * sizeof(T2));
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
+    unsigned char* stage0 = smem_raw + 128;
+    const int c = threadIdx.x % TX;
+    const int t = threadIdx.x / TX;
+    const int ntx = (a.nxh + TX - 1) / TX;
+    const long long per_comp = (long long)ntx * a.nz;
+    const long long ntiles = 3 * per_comp;
+    const T2* tw = tw_of<T>(a, 1);
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    auto issue = [&](long long tile, int st) {
+        const int cc = (int)(tile / per_comp);
+        const long long r = tile - cc * per_comp;
+        const int z = (int)(r / ntx);
+        const int k0 = (int)(r % ntx) * TX;
+        mbar_arrive_expect_tx(&bars[st], TILE_BYTES);
+        tma_load_4d(stage0 + st * STAGE, &spec_map, 2 * k0, 0, z, cc, &bars[st]);
+    };
+    long long tile = blockIdx.x;
+    if (threadIdx.x == 0 && tile < ntiles) issue(tile, 0);
+    for (int i = 0; tile < ntiles; tile += gridDim.x, ++i) {
+        const int st = i & 1;
+        const long long next = tile + gridDim.x;
+        if (threadIdx.x == 0 && next < ntiles) {
+            fence_proxy_async_smem();
+            issue(next, st ^ 1);
+        }
+        if (!tma_pipeline_wait<T2>(bars, i, st, next < ntiles, a.err)) return;
+        const int cc = (int)(tile / per_comp);
+        const long long r = tile - cc * per_comp;
+        const long long z = r / ntx;
+        const int k0 = (int)(r % ntx) * TX;
+        const bool act = k0 + c < a.nxh;
+        T2* blk = reinterpret_cast<T2*>(stage0 + st * STAGE);
+        T2* my = blk + c * LD;
+        const T2* rc = blk + c;
+        auto ld_raw = [&](int pos) { return rc[pos * TX]; };
+        T2* base = reinterpret_cast<T2*>(a.spec) + cc * a.nh + z * N * a.rs + k0 + (act ? c : 0);
+        const long long es = a.rs;
+        auto st_g = [&](int pos, T2 v) { base[pos * es] = v; };
+        if (S < 0) {
+            stage_a<R1, R2, -1, TPL, true>(my, t, act, tw, ld_raw);
+            __syncthreads();
+            stage_b<R1, R2, -1, TPL, false>(my, t, act, st_g);
+        } else {
+            stage_a<R2, R1, +1, TPL, true>(my, t, act, tw, ld_raw);
+            __syncthreads();
             stage_b<R2, R1, +1, TPL, false>(my, t, act, st_g);
         }
         __syncthreads();  // this stage is refilled by the issue of iteration i + 1
@@ -651,6 +760,18 @@ int col_ld_rt(int n) {
     }
 }
 
+// dynamic shared memory of the TMA-fed y pass: mbarriers + two stages
+template <typename T>
+size_t y_smem_rt(int n) {
+    constexpr int TX = col_tx<T>();
+    switch (n) {
+        case 32: return 128 + 2 * y_stage_bytes<T, 32, TX>();
+        case 64: return 128 + 2 * y_stage_bytes<T, 64, TX>();
+        case 128: return 128 + 2 * y_stage_bytes<T, 128, TX>();
+        default: return 128 + 2 * y_stage_bytes<T, 256, TX>();
+    }
+}
+
 // dynamic shared memory of the z pass: mbarriers + two pipeline stages
 template <typename T>
 size_t z_smem_rt(int n) {
@@ -673,6 +794,12 @@ cudaError_t run_y(int n, int dir, const FastArgs& a, dim3 grid, cudaStream_t s);
 template <typename T>
 cudaError_t run_z(int n, const CUtensorMap& spec_map, const CUtensorMap& green_map, const FastArgs& a,
                   dim3 grid, size_t smem, cudaStream_t s);
+template <typename T>
+cudaError_t run_y_tma(int n, int dir, const CUtensorMap& spec_map, const FastArgs& a, int grid,
+                      size_t smem, cudaStream_t s);
+// blocks of the TMA-fed y kernel resident per SM at this shared-memory size
+template <typename T>
+int y_blocks_per_sm(int n, size_t smem);
 // blocks of the x kernels resident per SM at this shared-memory size
 template <typename T>
 int x_blocks_per_sm(int n, bool inverse, int threads, size_t smem);
