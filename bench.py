@@ -739,6 +739,32 @@ def run_brinkman(args):
         cpu = {"value": t_cpu * its, "unit": "s", "cores": 1, "kind": "port",
                "sample": "C restatement of the reference iteration, %d iterations at 128^3 "
                          "timed (%.3f s each), scaled to %d" % (k, t_cpu, its)}
+    # config C2 compares the Brinkman permeability with the variational method
+    # on the same geometry (the reference runs both behind one runner,
+    # PermeabilityRunner.cpp:250-447 and :451-832): the variational K (FP64,
+    # tol 1e-10) and the Brinkman fixed point's K for all three load cases
+    from fft_method_test_gb300.permeability import (PermeabilityProblem,
+                                                    computePermeabilityTensorFixedPoint)
+
+    t0 = time.perf_counter()
+    with PermeabilityProblem(mask.shape, precision="fp64") as pv:
+        pv.set_geometry(mask)
+        K_var, st_var = pv.solve_permeability(TOL_FP64, MAXIT)
+    t_var = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    K_br, st_br = computePermeabilityTensorFixedPoint(ids, solid_penalty=1e4, tolerance=1e-8)
+    t_brk = time.perf_counter() - t0
+    fx = oracle_fixture("c2_128_sph", mask)
+    comparison = {
+        "variational": {"K": np.asarray(K_var).tolist(), "tol": TOL_FP64, "seconds": t_var,
+                        "iterations": [s["iterations"] for s in st_var],
+                        "K_rel_err_vs_oracle": (float(np.linalg.norm(K_var - fx["K"]) /
+                                                      np.linalg.norm(fx["K"])) if fx else None)},
+        "brinkman_fixed_point": {"K": np.asarray(K_br).tolist(), "tol": 1e-8, "seconds": t_brk,
+                                 "iterations": [s["iterations"] for s in st_br]},
+        "K_rel_diff_brinkman_vs_variational": float(np.linalg.norm(np.asarray(K_br) - K_var) /
+                                                    np.linalg.norm(K_var)),
+    }
     line = {"metric": "brinkman_c2_128", "data": "synthetic", "n_gpus": 1, "dtype": "fp64",
             "config": {"workload": "spheres128_r8_phi0.45_seed1002", "penalty": 1e4, "mu": 1.0,
                        "force": [1.0, 0.0, 0.0]},
@@ -754,6 +780,7 @@ def run_brinkman(args):
             "fixed_point": {"tol": 1e-8, "iterations": fpnt["iterations"], "seconds": t_fp,
                             "converged": bool(fpnt["converged"]), "residual": fpnt["residual"],
                             "U": [float(u) for u in U_fp]},
+            "c2_comparison": comparison,
             "cpu_baseline": cpu}
     print(json.dumps(line), flush=True)
 

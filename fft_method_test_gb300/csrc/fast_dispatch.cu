@@ -51,6 +51,7 @@ static cudaError_t fast_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     // x passes: tiles of `rows` grid rows, persistent over the tiles
     // grid rows per tile: the tuned cap when set (even), else about 192 threads
     int rows = P.x_rows > 0 ? std::max(2, P.x_rows & ~1) : fast::x_rows_for(P.nx);
+    rows = std::min(rows, 2 * fast::kMaxXLines / 3);
     if (rows > P.nrows) rows = (int)((P.nrows + 1) & ~1LL);
     a.rows = rows;
     a.ntiles = (P.nrows + rows - 1) / rows;

@@ -253,6 +253,18 @@ __device__ __forceinline__ void cp_async_wait() {
 
 // ---- P1: scatter + R2C x -------------------------------------------------------
 
+// complex lines per tile of the x passes at most (3 * rows / 2, rows <= 32)
+constexpr int kMaxXLines = 48;
+
+// two neighbouring complex values to 16-byte aligned global memory
+__device__ __forceinline__ void store_pair(float2* p, float2 a, float2 b) {
+    *reinterpret_cast<float4*>(p) = make_float4(a.x, a.y, b.x, b.y);
+}
+__device__ __forceinline__ void store_pair(double2* p, double2 a, double2 b) {
+    p[0] = a;
+    p[1] = b;
+}
+
 template <typename T, int N>
 __global__ void __launch_bounds__(384) k_fx_fwd(FastArgs a) {
     if (a.skip && *a.skip) return;
@@ -261,6 +273,7 @@ __global__ void __launch_bounds__(384) k_fx_fwd(FastArgs a) {
     constexpr int LD = x_ld<N, T>();
     constexpr int NH = N / 2 + 1;
     extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ long long dst_a[kMaxXLines], dst_b[kMaxXLines];
     T2* lines = reinterpret_cast<T2*>(smem_raw);
     const int RB = a.rows;
     const int nq = 3 * RB / 2;
@@ -313,22 +326,34 @@ __global__ void __launch_bounds__(384) k_fx_fwd(FastArgs a) {
             stage_b<R1, R2, -1, TPL, true>(my, t, act, st_nat);
         }
         __syncthreads();
-        // 4) separate the two real spectra of each complex line, store the half spectra
-        for (int it = tid; it < nqa * NH; it += nthr) {
-            const int qq = it / NH;
-            const int k = it - qq * NH;
-            const T2 zk = lines[qq * LD + k];
-            const T2 zn = lines[qq * LD + (k == 0 ? 0 : N - k)];
-            const T h = (T)0.5;
-            const T2 A = cmk<T2>(h * (zk.x + zn.x), h * (zk.y - zn.y));
-            const T2 B = cmk<T2>(h * (zk.y + zn.y), h * (zn.x - zk.x));
-            const int La = 2 * qq, rla = La / 3, ca = La - 3 * rla;
-            spec[ca * a.nh + (r0 + rla) * a.rs + k] = A;
-            const int Lb = La + 1;
-            if (Lb < nreal) {
-                const int rlb = Lb / 3, cb = Lb - 3 * rlb;
-                spec[cb * a.nh + (r0 + rlb) * a.rs + k] = B;
+        // 4) separate the two real spectra of each complex line, store the half
+        //    spectra, two neighbouring kx per thread (one 16-byte store for
+        //    FP32; rs is a multiple of 4, so every even kx is 16-byte aligned;
+        //    kx = N/2 + 1 lands in the row padding)
+        if (tid < nqa) {
+            const int La = 2 * tid, rla = La / 3, ca = La - 3 * rla;
+            dst_a[tid] = ca * a.nh + (r0 + rla) * a.rs;
+            const int Lb = La + 1, rlb = Lb / 3, cb = Lb - 3 * rlb;
+            dst_b[tid] = Lb < nreal ? cb * a.nh + (r0 + rlb) * a.rs : -1;
+        }
+        __syncthreads();
+        constexpr int NP = (NH + 1) / 2;
+        for (int it = tid; it < nqa * NP; it += nthr) {
+            const int qq = it / NP;
+            const int k = 2 * (it - qq * NP);
+            const T2* ln = lines + qq * LD;
+            T2 A[2], B[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int kk = k + e;
+                const T2 zk = ln[kk];
+                const T2 zn = ln[kk == 0 ? 0 : N - kk];
+                const T h = (T)0.5;
+                A[e] = cmk<T2>(h * (zk.x + zn.x), h * (zk.y - zn.y));
+                B[e] = cmk<T2>(h * (zk.y + zn.y), h * (zn.x - zk.x));
             }
+            store_pair(spec + dst_a[qq] + k, A[0], A[1]);
+            if (dst_b[qq] >= 0) store_pair(spec + dst_b[qq] + k, B[0], B[1]);
         }
         __syncthreads();
     }
