@@ -68,27 +68,26 @@ static cudaError_t fast_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     int xgrid_i = (int)std::min<long long>(a.ntiles, (long long)inv_per_sm * P.sm_count);
     xgrid_i = std::min(xgrid_i, kMaxPartials);
 
-    // column passes
+    // y passes: TX kx columns of one z plane and one component per CTA
     constexpr int TX = fast::col_tx<T>();
     const int ntx = (P.nxh + TX - 1) / TX;
+    const dim3 ygrid(ntx, P.nz, 3);
+    // z pass: persistent, TMA-fed, two pipeline stages per CTA
+    constexpr int TZ = fast::z_tx<T>();
     const CUtensorMap* smap = nullptr;
     const CUtensorMap* gmap = nullptr;
-    const CUtensorMap* ymap = nullptr;
-    if (!fast_maps(P, sizeof(T) == 8, TX, &smap, &gmap, &ymap)) return cudaErrorNotSupported;
-    // y passes: persistent TMA-fed CTAs, as many as fit per SM
-    const size_t ysmem = fast::y_smem_rt<T>(P.ny);
-    const int ygrid = (int)std::min<long long>(
-        (long long)3 * ntx * P.nz, (long long)fast::y_blocks_per_sm<T>(P.ny, ysmem) * P.sm_count);
-    // z pass: persistent, one CTA per SM (two pipeline stages of about 100 KB)
-    const dim3 zgrid((unsigned)std::min<long long>((long long)ntx * P.ny, P.sm_count), 1, 1);
+    if (!fast_maps(P, sizeof(T) == 8, TZ, &smap, &gmap)) return cudaErrorNotSupported;
     const size_t zsmem = fast::z_smem_rt<T>(P.nz);
+    const int ntz = (P.nxh + TZ - 1) / TZ;
+    const int zgrid = (int)std::min<long long>(
+        (long long)ntz * P.ny, (long long)fast::z_blocks_per_sm<T>(P.nz, zsmem) * P.sm_count);
 
     cudaStream_t st = P.stream;
     cudaError_t e;
     if ((e = fast::run_xfwd<T>(P.nx, a, xgrid_f, xthreads, xsmem, st)) != cudaSuccess) return e;
-    if ((e = fast::run_y_tma<T>(P.ny, -1, *ymap, a, ygrid, ysmem, st)) != cudaSuccess) return e;
-    if ((e = fast::run_z<T>(P.nz, *smap, *gmap, a, zgrid, zsmem, st)) != cudaSuccess) return e;
-    if ((e = fast::run_y_tma<T>(P.ny, +1, *ymap, a, ygrid, ysmem, st)) != cudaSuccess) return e;
+    if ((e = fast::run_y<T>(P.ny, -1, a, ygrid, st)) != cudaSuccess) return e;
+    if ((e = fast::run_z<T>(P.nz, *smap, *gmap, a, dim3(zgrid), zsmem, st)) != cudaSuccess) return e;
+    if ((e = fast::run_y<T>(P.ny, +1, a, ygrid, st)) != cudaSuccess) return e;
     if ((e = fast::run_xinv<T>(P.nx, a, stage_bytes, xgrid_i, xthreads, xismem, st)) != cudaSuccess)
         return e;
     *nparts = xgrid_i;

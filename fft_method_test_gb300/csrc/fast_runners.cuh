@@ -51,7 +51,7 @@ cudaError_t run_y(int n, int dir, const FastArgs& a, dim3 grid, cudaStream_t s) 
 template <typename T>
 cudaError_t run_z(int n, const CUtensorMap& spec_map, const CUtensorMap& green_map, const FastArgs& a,
                   dim3 grid, size_t smem, cudaStream_t s) {
-    constexpr int TX = col_tx<T>();
+    constexpr int TX = z_tx<T>();
 #define FP_CALL(N) FP_RUN((k_fz<T, N, TX>), grid, 3 * TX * Split<N>::R2, smem, s, spec_map, green_map, a)
     FP_FAST_SWITCH(n, FP_CALL)
 #undef FP_CALL
@@ -59,30 +59,15 @@ cudaError_t run_z(int n, const CUtensorMap& spec_map, const CUtensorMap& green_m
 }
 
 template <typename T>
-cudaError_t run_y_tma(int n, int dir, const CUtensorMap& spec_map, const FastArgs& a, int grid,
-                      size_t smem, cudaStream_t s) {
-    constexpr int TX = col_tx<T>();
-#define FP_CALL(N)                                                                           \
-    if (dir < 0)                                                                             \
-        FP_RUN((k_fy<T, N, -1, TX>), grid, TX * Split<N>::R2, smem, s, spec_map, a);         \
-    else                                                                                     \
-        FP_RUN((k_fy<T, N, +1, TX>), grid, TX * Split<N>::R2, smem, s, spec_map, a)
-    FP_FAST_SWITCH(n, FP_CALL)
-#undef FP_CALL
-    return cudaGetLastError();
-}
-
-template <typename T>
-int y_blocks_per_sm(int n, size_t smem) {
-    constexpr int TX = col_tx<T>();
+int z_blocks_per_sm(int n, size_t smem) {
+    constexpr int TX = z_tx<T>();
     int nb = 0;
 #define FP_CALL(N)                                                                            \
     {                                                                                         \
-        static std::atomic<unsigned long long> f_{0}, i_{0};                                  \
-        ensure_max_smem(k_fy<T, N, -1, TX>, f_);                                              \
-        ensure_max_smem(k_fy<T, N, +1, TX>, i_);                                              \
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fy<T, N, -1, TX>,                \
-                                                      TX * Split<N>::R2, smem);               \
+        static std::atomic<unsigned long long> f_{0};                                         \
+        ensure_max_smem(k_fz<T, N, TX>, f_);                                                  \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fz<T, N, TX>,                    \
+                                                      3 * TX * Split<N>::R2, smem);           \
     }
     switch (n) {
         case 32: FP_CALL(32); break;
@@ -127,9 +112,7 @@ int x_blocks_per_sm(int n, bool inverse, int threads, size_t smem) {
     template cudaError_t run_z<T>(int, const CUtensorMap&, const CUtensorMap&, const FastArgs&, dim3, \
                                   size_t, cudaStream_t);                                            \
     template int x_blocks_per_sm<T>(int, bool, int, size_t);                                      \
-    template cudaError_t run_y_tma<T>(int, int, const CUtensorMap&, const FastArgs&, int, size_t,  \
-                                      cudaStream_t);                                               \
-    template int y_blocks_per_sm<T>(int, size_t);
+    template int z_blocks_per_sm<T>(int, size_t);
 
 }  // namespace fast
 }  // namespace fp

@@ -21,9 +21,7 @@
 // Passes (kernels below):
 //   k_fx_fwd   scatter of the compact vector (minus its mean) into real
 //              x-lines, two real lines per complex FFT, half spectrum out
-//   k_fy       y pass, one component per tile of TX kx columns; persistent
-//              CTAs with a two-stage TMA pipeline (k_fcol_y: the same pass
-//              reading HBM directly, where TMA is off)
+//   k_fcol_y   y pass, one component per CTA slice, TX kx columns per CTA
 //   k_fz       z pass: forward, 3x3 Green multiply, inverse, all three
 //              components in one CTA; persistent CTAs with a two-stage TMA
 //              pipeline (cp.async.bulk.tensor boxes of the spectral and Green
@@ -39,6 +37,8 @@
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include "common.cuh"
 #include "fft_engine.cuh"
@@ -99,12 +99,15 @@ __host__ __device__ constexpr int line_span() {
     return N + Split<N>::R1;
 }
 
-// Column passes (thread = column + TX * (owner + TPL * comp)): FP32 lines
-// need stride = 2 mod 16 elements (a half-warp = 8 columns x 2 owners),
-// FP64 lines an odd stride (a quarter-warp = TX <= 8 columns of one owner).
-template <int N, typename T>
+// Column passes (thread = column + TX * (owner + TPL * comp)): one
+// shared-memory wavefront serves G = 128 / sizeof(complex) threads (a
+// half-warp in FP32, a quarter-warp in FP64), TX columns x G / TX
+// consecutive owners; every exchange steps owners by an odd number of
+// elements, so a line stride of G / TX modulo G keeps them in distinct banks.
+template <int N, typename T, int TX>
 __host__ __device__ constexpr int col_ld() {
-    return sizeof(T) == 4 ? ((line_span<N>() + 13) / 16) * 16 + 2 : (line_span<N>() | 1);
+    constexpr int G = 128 / (2 * (int)sizeof(T));
+    return ((line_span<N>() + G - 1) / G) * G + (G / TX) % G;
 }
 
 // x passes (thread = owner + TPL * line): the lines of one half-warp (FP32)
@@ -131,6 +134,17 @@ struct GroupBarrier {
         asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
     }
 };
+
+template <class B>
+__device__ __forceinline__ B make_group_barrier(int id, int count);
+template <>
+__device__ __forceinline__ GroupBarrier make_group_barrier<GroupBarrier>(int id, int count) {
+    return GroupBarrier{id, count};
+}
+template <>
+__device__ __forceinline__ CtaBarrier make_group_barrier<CtaBarrier>(int, int) {
+    return CtaBarrier{};
+}
 
 // ---- four-step stages --------------------------------------------------------
 
@@ -492,7 +506,7 @@ __global__ void __launch_bounds__(TX * Split<N>::R2) k_fcol_y(FastArgs a) {
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
     constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = R2;
-    constexpr int LD = col_ld<N, T>();
+    constexpr int LD = col_ld<N, T, TX>();
     __shared__ __align__(16) T2 lines[TX * LD];
     const int c = threadIdx.x % TX;
     const int t = threadIdx.x / TX;
@@ -523,7 +537,8 @@ __global__ void __launch_bounds__(TX * Split<N>::R2) k_fcol_y(FastArgs a) {
 // starts 128-byte aligned (a TMA destination) and the blocks never overlap.
 template <typename T, int N, int TX>
 __host__ __device__ constexpr int comp_stride() {
-    return (int)(((size_t)TX * col_ld<N, T>() * 2 * sizeof(T) + 127) / 128 * 128 / (2 * sizeof(T)));
+    return (int)(((size_t)TX * col_ld<N, T, TX>() * 2 * sizeof(T) + 127) / 128 * 128 /
+                 (2 * sizeof(T)));
 }
 
 // Shared memory of one pipeline stage of the z pass: the spectral tile (per
@@ -554,7 +569,7 @@ __global__ void __launch_bounds__(3 * TX * Split<N>::R2, 1)
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
     constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = R2;
-    constexpr int LD = col_ld<N, T>();
+    constexpr int LD = col_ld<N, T, TX>();
     constexpr int CS = comp_stride<T, N, TX>();
     constexpr size_t STAGE = z_stage_bytes<T, N, TX>();
     constexpr size_t GOFF = z_green_offset<T, N, TX>();
@@ -565,7 +580,9 @@ __global__ void __launch_bounds__(3 * TX * Split<N>::R2, 1)
     const int c = threadIdx.x % TX;
     const int t = (threadIdx.x / TX) % TPL;
     const int comp = threadIdx.x / (TX * TPL);
-    const GroupBarrier gbar{1 + comp, TX * TPL};
+    // a named barrier per component needs whole warps per component
+    using GBar = typename std::conditional<(TX * TPL) % 32 == 0, GroupBarrier, CtaBarrier>::type;
+    GBar gbar = make_group_barrier<GBar>(1 + comp, TX * TPL);
     const int ntx = (a.nxh + TX - 1) / TX;
     const long long ntiles = (long long)ntx * a.ny;
     const T2* tw = tw_of<T>(a, 2);
@@ -645,86 +662,6 @@ __global__ void __launch_bounds__(3 * TX * Split<N>::R2, 1)
     }
 }
 
-// ---- P2 / P4: y pass fed by TMA ------------------------------------------------
-
-// One pipeline stage of the y pass: the raw box [ny][TX] of one component,
-// overwritten in place by the padded lines [TX][LD].
-template <typename T, int N, int TX>
-__host__ __device__ constexpr size_t y_stage_bytes() {
-    return (size_t)comp_stride<T, N, TX>() * 2 * sizeof(T);
-}
-
-// Persistent CTAs walk the (kx tile, z plane, component) tiles; thread =
-// column + TX * owner.  While tile i is transformed, the TMA engine brings
-// the {2 TX reals, ny} box of tile i + 1 into the other stage.  The last
-// stage writes HBM directly.  Bounded waits as in k_fz.
-template <typename T, int N, int S, int TX>
-__global__ void __launch_bounds__(TX * Split<N>::R2)
-    k_fy(const __grid_constant__ CUtensorMap spec_map, FastArgs a) {
-    if (a.skip && *a.skip) return;
-    using T2 = c_t<T>;
-    constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = R2;
-    constexpr int LD = col_ld<N, T>();
-    constexpr size_t STAGE = y_stage_bytes<T, N, TX>();
-    constexpr uint32_t TILE_BYTES = (uint32_t)(N * TX * sizeof(T2));
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
-    unsigned char* stage0 = smem_raw + 128;
-    const int c = threadIdx.x % TX;
-    const int t = threadIdx.x / TX;
-    const int ntx = (a.nxh + TX - 1) / TX;
-    const long long per_comp = (long long)ntx * a.nz;
-    const long long ntiles = 3 * per_comp;
-    const T2* tw = tw_of<T>(a, 1);
-    if (threadIdx.x == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-    auto issue = [&](long long tile, int st) {
-        const int cc = (int)(tile / per_comp);
-        const long long r = tile - cc * per_comp;
-        const int z = (int)(r / ntx);
-        const int k0 = (int)(r % ntx) * TX;
-        mbar_arrive_expect_tx(&bars[st], TILE_BYTES);
-        tma_load_4d(stage0 + st * STAGE, &spec_map, 2 * k0, 0, z, cc, &bars[st]);
-    };
-    long long tile = blockIdx.x;
-    if (threadIdx.x == 0 && tile < ntiles) issue(tile, 0);
-    for (int i = 0; tile < ntiles; tile += gridDim.x, ++i) {
-        const int st = i & 1;
-        const long long next = tile + gridDim.x;
-        if (threadIdx.x == 0 && next < ntiles) {
-            fence_proxy_async_smem();
-            issue(next, st ^ 1);
-        }
-        if (!tma_pipeline_wait<T2>(bars, i, st, next < ntiles, a.err)) return;
-        const int cc = (int)(tile / per_comp);
-        const long long r = tile - cc * per_comp;
-        const long long z = r / ntx;
-        const int k0 = (int)(r % ntx) * TX;
-        const bool act = k0 + c < a.nxh;
-        T2* blk = reinterpret_cast<T2*>(stage0 + st * STAGE);
-        T2* my = blk + c * LD;
-        const T2* rc = blk + c;
-        auto ld_raw = [&](int pos) { return rc[pos * TX]; };
-        T2* base = reinterpret_cast<T2*>(a.spec) + cc * a.nh + z * N * a.rs + k0 + (act ? c : 0);
-        const long long es = a.rs;
-        auto st_g = [&](int pos, T2 v) { base[pos * es] = v; };
-        if (S < 0) {
-            stage_a<R1, R2, -1, TPL, true>(my, t, act, tw, ld_raw);
-            __syncthreads();
-            stage_b<R1, R2, -1, TPL, false>(my, t, act, st_g);
-        } else {
-            stage_a<R2, R1, +1, TPL, true>(my, t, act, tw, ld_raw);
-            __syncthreads();
-            stage_b<R2, R1, +1, TPL, false>(my, t, act, st_g);
-        }
-        __syncthreads();  // this stage is refilled by the issue of iteration i + 1
-    }
-}
-
 }  // namespace fast
 
 // Runs the five passes with the specialised kernels when the grid, the
@@ -740,10 +677,15 @@ cudaError_t fast_apply(Problem& P, int precision, const ApplyArgs& aa, int* npar
 namespace fp {
 namespace fast {
 
-// kx columns per CTA of the column passes: 64-byte row segments
+// kx columns per CTA of the y pass (64-byte row segments) and per tile of the
+// z pass (32-byte spectral rows, 16-byte FP32 Green rows: two CTAs per SM)
 template <typename T>
 constexpr int col_tx() {
     return sizeof(T) == 4 ? 8 : 4;
+}
+template <typename T>
+constexpr int z_tx() {
+    return 4;
 }
 
 // grid edges with specialised kernels
@@ -775,32 +717,11 @@ int x_ld_rt(int n) {
         default: return x_ld<256, T>();
     }
 }
-template <typename T>
-int col_ld_rt(int n) {
-    switch (n) {
-        case 32: return col_ld<32, T>();
-        case 64: return col_ld<64, T>();
-        case 128: return col_ld<128, T>();
-        default: return col_ld<256, T>();
-    }
-}
-
-// dynamic shared memory of the TMA-fed y pass: mbarriers + two stages
-template <typename T>
-size_t y_smem_rt(int n) {
-    constexpr int TX = col_tx<T>();
-    switch (n) {
-        case 32: return 128 + 2 * y_stage_bytes<T, 32, TX>();
-        case 64: return 128 + 2 * y_stage_bytes<T, 64, TX>();
-        case 128: return 128 + 2 * y_stage_bytes<T, 128, TX>();
-        default: return 128 + 2 * y_stage_bytes<T, 256, TX>();
-    }
-}
 
 // dynamic shared memory of the z pass: mbarriers + two pipeline stages
 template <typename T>
 size_t z_smem_rt(int n) {
-    constexpr int TX = col_tx<T>();
+    constexpr int TX = z_tx<T>();
     switch (n) {
         case 32: return 128 + 2 * z_stage_bytes<T, 32, TX>();
         case 64: return 128 + 2 * z_stage_bytes<T, 64, TX>();
@@ -819,12 +740,10 @@ cudaError_t run_y(int n, int dir, const FastArgs& a, dim3 grid, cudaStream_t s);
 template <typename T>
 cudaError_t run_z(int n, const CUtensorMap& spec_map, const CUtensorMap& green_map, const FastArgs& a,
                   dim3 grid, size_t smem, cudaStream_t s);
+// blocks of the z kernel resident per SM at this shared-memory size
 template <typename T>
-cudaError_t run_y_tma(int n, int dir, const CUtensorMap& spec_map, const FastArgs& a, int grid,
-                      size_t smem, cudaStream_t s);
-// blocks of the TMA-fed y kernel resident per SM at this shared-memory size
-template <typename T>
-int y_blocks_per_sm(int n, size_t smem);
+int z_blocks_per_sm(int n, size_t smem);
+
 // blocks of the x kernels resident per SM at this shared-memory size
 template <typename T>
 int x_blocks_per_sm(int n, bool inverse, int threads, size_t smem);

@@ -135,7 +135,7 @@ struct Problem {
     TmaCache tma_y[2], tma_z[2];
     // specialised z pass: tensor maps of the spectral field and the Green
     // table [precision 0 = FP64, 1 = FP32], keyed by the table's address
-    CUtensorMap fz_spec_map[2], fz_green_map[2], fy_spec_map[2];
+    CUtensorMap fz_spec_map[2], fz_green_map[2];
     const void* fz_green_ptr[2] = {nullptr, nullptr};
     bool fz_valid[2] = {false, false};
     // MINRES iteration chunks replayed as CUDA graphs (FFTPERM_NO_GRAPHS=1: off).
@@ -181,13 +181,11 @@ cudaError_t launch_support(Problem& P);
 // Computes the Green table into g64 and/or g32 (either may be null).
 cudaError_t launch_green(Problem& P, double* g64, float* g32);
 
-// Tensor maps of the specialised y and z passes (kernels_fft.cu): the
-// spectral field as [3][nz][ny][2*nxh] reals with boxes {2*tx, 1, nz, 1} (z)
-// and {2*tx, ny, 1, 1} (y), the Green table as [6][nz][ny][nxh] with boxes
-// {tx, 1, nz, 1}.  false when TMA is unavailable or the layout does not
-// qualify.
-bool fast_maps(Problem& P, bool dbl, int tx, const CUtensorMap** spec_z, const CUtensorMap** green,
-               const CUtensorMap** spec_y);
+// Tensor maps of the specialised z pass (kernels_fft.cu): the spectral field
+// as [3][nz][ny][2*nxh] reals with boxes {2*tx, 1, nz, 1} and the Green table
+// as [6][nz][ny][nxh] with boxes {tx, 1, nz, 1}.  false when TMA is
+// unavailable or the layout does not qualify.
+bool fast_maps(Problem& P, bool dbl, int tx, const CUtensorMap** spec, const CUtensorMap** green);
 
 // ---- operator passes (kernels_fft.cu) ----
 // Source of the forward x pass.

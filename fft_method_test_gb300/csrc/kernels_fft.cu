@@ -203,12 +203,11 @@ static bool tma_setup(Problem& P, bool dbl, int axis, int tpl, int padsh, TmaTil
     return true;
 }
 
-bool fast_maps(Problem& P, bool dbl, int tx, const CUtensorMap** spec, const CUtensorMap** green,
-               const CUtensorMap** spec_y) {
+bool fast_maps(Problem& P, bool dbl, int tx, const CUtensorMap** spec, const CUtensorMap** green) {
     if (!tma_encoder()) return false;
     const int k = dbl ? 0 : 1;
     const void* g = dbl ? (const void*)P.d_green64 : (const void*)P.d_green32;
-    if (!g || P.nz > 256 || P.ny > 256) return false;
+    if (!g || P.nz > 256) return false;
     if (!P.fz_valid[k] || P.fz_green_ptr[k] != g) {
         const size_t e = dbl ? sizeof(double) : sizeof(float);
         const CUtensorMapDataType dt = dbl ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
@@ -221,11 +220,6 @@ bool fast_maps(Problem& P, bool dbl, int tx, const CUtensorMap** spec, const CUt
         CUresult r = tma_encoder()(&P.fz_spec_map[k], dt, 4, P.d_spec, sd, ss, sb, estr,
                                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                    CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if (r != CUDA_SUCCESS) return false;
-        const cuuint32_t yb[4] = {(cuuint32_t)(2 * tx), (cuuint32_t)P.ny, 1u, 1u};
-        r = tma_encoder()(&P.fy_spec_map[k], dt, 4, P.d_spec, sd, ss, yb, estr,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) return false;
         // the Green table: six real blocks
         const cuuint64_t gd[4] = {(cuuint64_t)P.nxh, (cuuint64_t)P.ny, (cuuint64_t)P.nz, 6};
@@ -241,7 +235,6 @@ bool fast_maps(Problem& P, bool dbl, int tx, const CUtensorMap** spec, const CUt
     }
     *spec = &P.fz_spec_map[k];
     *green = &P.fz_green_map[k];
-    *spec_y = &P.fy_spec_map[k];
     return true;
 }
 
