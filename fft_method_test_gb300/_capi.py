@@ -39,7 +39,8 @@ EXPORTED = [
     "fp_kernel_launch_count", "fp_brinkman_fft_solve", "fp_brinkman_fft_permeability",
     "fp_autotune", "fp_set_tiling", "fp_batch_solve_permeability", "fp_batch_last_error", "fp_write_fvel",
     "fp_nn_conv", "fp_nn_wgrad", "fp_nn_bias_grad", "fp_nn_relu_back", "fp_nn_adam", "fp_nn_loss",
-    "fp_measure_fp64_rate",
+    "fp_measure_fp64_rate", "fp_nn_conv_tc", "fp_nn_tc_error", "fp_nn_pool2", "fp_nn_pool2_back",
+    "fp_nn_up2_add", "fp_nn_up2_add_back", "fp_nn_wgrad_cc",
 ]
 
 
@@ -123,6 +124,20 @@ _SIGNATURES = {
     "fp_nn_conv": ([C.c_int, C.c_int, C.c_int, C.c_int64, C.c_int, C.c_int, C.c_void_p, C.c_int,
                     C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p],
                    C.c_int),
+    "fp_nn_conv_tc": ([C.c_int, C.c_int, C.c_int, C.c_int64, C.c_int, C.c_int, C.c_void_p, C.c_int,
+                       C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p],
+                      C.c_int),
+    "fp_nn_tc_error": ([C.POINTER(C.c_int), C.c_int], C.c_int),
+    "fp_nn_pool2": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p],
+                    C.c_int),
+    "fp_nn_pool2_back": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                          C.c_void_p], C.c_int),
+    "fp_nn_up2_add": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                       C.c_void_p, C.c_void_p], C.c_int),
+    "fp_nn_up2_add_back": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                            C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "fp_nn_wgrad_cc": ([C.c_int, C.c_int, C.c_int, C.c_int64, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                        C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "fp_nn_wgrad": ([C.c_int, C.c_int, C.c_int, C.c_int64, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
                      C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "fp_nn_bias_grad": ([C.c_void_p, C.c_int64, C.c_int, C.c_void_p, C.c_void_p], C.c_int),

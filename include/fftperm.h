@@ -224,8 +224,36 @@ const char* fp_batch_last_error(void);
 int fp_nn_conv(int nx, int ny, int nz, int64_t total, int dilation, int sign, const void* in_bf16,
                int cin, const void* w_bf16, const float* bias, int cout, int relu, float* out_f32,
                void* out_bf16, void* stream);
+/* fp_nn_conv on the fifth-generation tensor cores (tcgen05.mma, accumulator
+ * in tensor memory): the same arguments and results, cin % 16 == 0 and
+ * cin <= 128, cout in {16, 32, 64, 128}.  A bounded wait that gives up sets
+ * a flag that fp_nn_tc_error reads (and clears with reset != 0). */
+int fp_nn_conv_tc(int nx, int ny, int nz, int64_t total, int dilation, int sign,
+                  const void* in_bf16, int cin, const void* w_bf16, const float* bias, int cout,
+                  int relu, float* out_f32, void* out_bf16, void* stream);
+int fp_nn_tc_error(int* flag, int reset);
 int fp_nn_wgrad(int nx, int ny, int nz, int64_t total, int dilation, const void* dy_bf16, int cout,
                 const void* x_bf16, int cin, int64_t chunk, float* partial, float* dw, void* stream);
+/* The multi-level pieces of the U-Net (fine grid nx, ny, nz even; the coarse
+ * grid is half of it along each axis; BF16 or FP32 channels-last tensors of
+ * `samples` stacked cells):
+ * fp_nn_pool2: coarse = mean of the 8 children;
+ * fp_nn_pool2_back: dfine += dcoarse(parent) / 8;
+ * fp_nn_up2_add: out = act(coarse(parent) + skip), act = ReLU when relu;
+ * fp_nn_up2_add_back: with d = dout masked where post <= 0 (post may be
+ *   NULL: no mask), dskip = d and dcoarse = sum of d over the 8 children;
+ * fp_nn_wgrad_cc: fp_nn_wgrad on the CUDA cores for any cout, cin that are
+ *   multiples of 16; `partial` holds ceil(total/chunk) * 27 * cout * cin floats. */
+int fp_nn_pool2(int nx, int ny, int nz, int samples, int c, const void* in_bf16, void* out_bf16,
+                void* stream);
+int fp_nn_pool2_back(int nx, int ny, int nz, int samples, int c, const float* dcoarse, float* dfine,
+                     void* stream);
+int fp_nn_up2_add(int nx, int ny, int nz, int samples, int c, const void* coarse_bf16,
+                  const void* skip_bf16, int relu, void* out_bf16, void* stream);
+int fp_nn_up2_add_back(int nx, int ny, int nz, int samples, int c, const float* dout,
+                       const void* post_bf16, float* dskip, float* dcoarse, void* stream);
+int fp_nn_wgrad_cc(int nx, int ny, int nz, int64_t total, int dilation, const void* dy_bf16, int cout,
+                   const void* x_bf16, int cin, int64_t chunk, float* partial, float* dw, void* stream);
 int fp_nn_bias_grad(const void* dy_bf16, int64_t total, int cout, float* db, void* stream);
 int fp_nn_relu_back(const float* dpost, const void* post_bf16, int64_t total, int c, int cpad,
                     void* out_bf16, void* stream);

@@ -184,3 +184,164 @@ def test_trained_network_lowers_the_initial_residual(gpu_lib):
         rel_u.append(r2)
     assert np.mean(rel_t) < np.mean(rel_u) - 0.05, (rel_t, rel_u)
     assert max(rel_t) < 1.0
+
+
+# ---------------------------------------------------------------------------
+# the tcgen05 convolution and the U-Net
+# ---------------------------------------------------------------------------
+
+def _conv_ref_torch(x, w, shape, dil, sign, bias, relu):
+    """Periodic 3x3x3 convolution in float64 (torch): y[v][o] = sum_tap
+    sum_i x[v + sign*dil*off(tap)][i] w[tap][o][i]."""
+    import torch
+
+    nz, ny, nx = shape
+    cin, cout = x.shape[1], w.shape[1]
+    S = x.shape[0] // (nx * ny * nz)
+    x5 = x.reshape(S, nz, ny, nx, cin).double()
+    out = torch.zeros(S, nz, ny, nx, cout, dtype=torch.float64)
+    s = sign * dil
+    for tap in range(27):
+        dz, dy, dx = tap // 9 - 1, (tap // 3) % 3 - 1, tap % 3 - 1
+        out += torch.roll(x5, shifts=(-s * dz, -s * dy, -s * dx), dims=(1, 2, 3)) @ w[tap].double().T
+    out = out.reshape(-1, cout)
+    if bias is not None:
+        out += bias.double()
+    return torch.clamp(out, min=0) if relu else out
+
+
+@pytest.mark.parametrize("cin,cout", [(16, 16), (16, 32), (32, 64), (64, 128), (128, 128), (128, 64),
+                                      (32, 16)])
+@pytest.mark.parametrize("shape,samples,dil,sign", [((8, 8, 8), 2, 1, 1), ((7, 5, 6), 1, 2, -1)])
+def test_conv_tcgen05_matches_reference(gpu_lib, cin, cout, shape, samples, dil, sign):
+    """fp_nn_conv_tc (tcgen05.mma, TMEM accumulator) against a float64 torch
+    convolution of the same BF16 inputs: FP32 output to 1e-5, BF16 output to
+    BF16 rounding; the error flag of the bounded waits stays clear."""
+    import ctypes as C
+
+    import torch
+
+    torch.manual_seed(cin * 7 + cout)
+    n = int(np.prod(shape))
+    x = torch.randn(samples * n, cin, device="cuda").to(torch.bfloat16)
+    w = (torch.randn(27, cout, cin, device="cuda") * 0.1).to(torch.bfloat16)
+    b = torch.randn(cout, device="cuda")
+    o32 = torch.full((samples * n, cout), float("nan"), device="cuda")
+    o16 = torch.empty((samples * n, cout), dtype=torch.bfloat16, device="cuda")
+    rc = gpu_lib.fp_nn_conv_tc(shape[2], shape[1], shape[0], samples * n, dil, sign,
+                               C.c_void_p(x.data_ptr()), cin, C.c_void_p(w.data_ptr()),
+                               C.c_void_p(b.data_ptr()), cout, 1, C.c_void_p(o32.data_ptr()),
+                               C.c_void_p(o16.data_ptr()), None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    flag = C.c_int(1)
+    assert gpu_lib.fp_nn_tc_error(C.byref(flag), 1) == 0 and flag.value == 0
+    want = _conv_ref_torch(x.float().cpu(), w.float().cpu(), shape, dil, sign, b.cpu(), True)
+    scale = float(want.abs().max())
+    assert float((o32.double().cpu() - want).abs().max()) < 1e-5 * scale
+    assert float((o16.double().cpu() - want).abs().max()) < 1e-2 * scale
+
+
+def _unet_ref_loss(params, feat, shape, tgt, sup, tn):
+    """The U-Net in float32 torch (autograd), with the BF16 roundings of the
+    GPU path at the same places; returns the summed relative squared error of
+    the mean-free prediction on the support (the fp_nn_loss definition)."""
+    import torch
+    import torch.nn.functional as F
+
+    def r16(t):
+        return t.to(torch.bfloat16).float()
+
+    def conv(name, x, s, relu):
+        w, b = params[name]
+        nz, ny, nx = s
+        cout, cin = w.shape[1], w.shape[2]
+        S = x.shape[0] // (nz * ny * nx)
+        x5 = x.reshape(S, nz, ny, nx, cin).permute(0, 4, 1, 2, 3)
+        x5 = F.pad(x5, (1, 1, 1, 1, 1, 1), mode="circular")
+        k = w.reshape(3, 3, 3, cout, cin).permute(3, 4, 0, 1, 2)
+        y = F.conv3d(x5, k) + b.view(1, -1, 1, 1, 1)
+        y = y.permute(0, 2, 3, 4, 1).reshape(-1, cout)
+        return torch.relu(y) if relu else y
+
+    def pool(x, s, c):
+        nz, ny, nx = s
+        S = x.shape[0] // (nz * ny * nx)
+        x5 = x.reshape(S, nz, ny, nx, c).permute(0, 4, 1, 2, 3)
+        return F.avg_pool3d(x5, 2).permute(0, 2, 3, 4, 1).reshape(-1, c)
+
+    def up_add(cz, skip, s, c):
+        nz, ny, nx = s
+        S = skip.shape[0] // (nz * ny * nx)
+        c5 = cz.reshape(S, nz // 2, ny // 2, nx // 2, c)
+        c5 = c5.repeat_interleave(2, 1).repeat_interleave(2, 2).repeat_interleave(2, 3)
+        return torch.relu(c5.reshape(-1, c) + skip)
+
+    s = [tuple(d >> l for d in shape) for l in range(4)]
+    e0 = r16(conv("enc0", feat, s[0], True))
+    p0 = r16(pool(e0, s[0], 16))
+    e1 = r16(conv("enc1", p0, s[1], True))
+    p1 = r16(pool(e1, s[1], 32))
+    e2 = r16(conv("enc2", p1, s[2], True))
+    p2 = r16(pool(e2, s[2], 64))
+    e3 = r16(conv("enc3", p2, s[3], True))
+    b3 = r16(conv("bott", e3, s[3], True))
+    c3 = r16(conv("dec3", b3, s[3], False))
+    u2 = r16(up_add(c3, e2, s[2], 64))
+    c2 = r16(conv("dec2", u2, s[2], False))
+    u1 = r16(up_add(c2, e1, s[1], 32))
+    c1 = r16(conv("dec1", u1, s[1], False))
+    u0 = r16(up_add(c1, e0, s[0], 16))
+    out = conv("head", u0, s[0], False)
+    n = int(np.prod(shape))
+    S = out.shape[0] // n
+    loss = 0.0
+    for k in range(S):
+        o = out[k * n:(k + 1) * n, :3]
+        m = sup[k * n:(k + 1) * n].bool()
+        om = o[m] - o[m].mean(dim=0)
+        loss = loss + ((om - tgt[k * n:(k + 1) * n][m]) ** 2).sum() / tn[k]
+    return loss
+
+
+def test_unet_gradients_match_torch_autograd(gpu_lib):
+    """The U-Net's forward and backward passes (tcgen05 convolutions and data
+    gradients, weight gradients, pooling, up-sampling with skips) against
+    torch autograd of the same network in FP32: loss to 1e-2 and every
+    weight gradient to 5e-2 relative (BF16 activations and gradients)."""
+    import torch
+
+    from fft_method_test_gb300 import learned as L
+
+    shape, samples = (16, 16, 16), 2
+    n = int(np.prod(shape))
+    net = L.UNetWarmStart(seed=3)
+    rng = np.random.default_rng(4)
+    masks = [G.spheres(16, 3.0, 0.6, seed=40 + k) for k in range(samples)]
+    sup = torch.zeros(samples * n, dtype=torch.uint8, device="cuda")
+    tgt = torch.zeros(samples * n, 3, device="cuda")
+    for k, m in enumerate(masks):
+        solid = np.flatnonzero(m.ravel() == 0)
+        sup[k * n + torch.tensor(solid, device="cuda")] = 1
+        t = rng.standard_normal((len(solid), 3)).astype(np.float32)
+        t -= t.mean(axis=0)
+        tgt[k * n + torch.tensor(solid, device="cuda")] = torch.tensor(t, device="cuda")
+    tn = torch.stack([(tgt[k * n:(k + 1) * n] ** 2).sum() for k in range(samples)]).float()
+    mask_t = torch.tensor(np.concatenate([m.ravel() for m in masks]), device="cuda")
+    feat = L.features_gpu(mask_t, sup)
+    out, saved = net.forward(feat, shape, samples, keep=True)
+    loss, dout = L.loss_and_grad(net, out, tgt, sup, tn, n, samples)
+    net.backward(dout, saved)
+    torch.cuda.synchronize()
+    params = {}
+    for name, p in net.params.items():
+        w = p["wf"].float().reshape(27, p["cout"], p["cin"]).clone().requires_grad_(True)
+        b = p["b"].clone().requires_grad_(True)
+        params[name] = (w, b)
+    ref = _unet_ref_loss(params, feat.float(), shape, tgt, sup, tn)
+    ref.backward()
+    assert abs(float(loss.sum()) - float(ref)) < 1e-2 * abs(float(ref))
+    for name, p in net.params.items():
+        gw = params[name][0].grad.reshape(-1)
+        err = float((p["gw"] - gw).abs().max() / gw.abs().max())
+        assert err < 5e-2, (name, err)
