@@ -308,7 +308,8 @@ def test_unet_gradients_match_torch_autograd(gpu_lib):
     """The U-Net's forward and backward passes (tcgen05 convolutions and data
     gradients, weight gradients, pooling, up-sampling with skips) against
     torch autograd of the same network in FP32: loss to 1e-2 and every
-    weight gradient to 5e-2 relative (BF16 activations and gradients)."""
+    weight gradient to 5e-2 in the relative 2-norm (the GPU path rounds
+    activations and the gradients between layers to BF16)."""
     import torch
 
     from fft_method_test_gb300 import learned as L
@@ -340,8 +341,8 @@ def test_unet_gradients_match_torch_autograd(gpu_lib):
         params[name] = (w, b)
     ref = _unet_ref_loss(params, feat.float(), shape, tgt, sup, tn)
     ref.backward()
-    assert abs(float(loss.sum()) - float(ref)) < 1e-2 * abs(float(ref))
+    assert abs(float(loss.sum()) - float(ref.detach())) < 1e-2 * abs(float(ref.detach()))
     for name, p in net.params.items():
         gw = params[name][0].grad.reshape(-1)
-        err = float((p["gw"] - gw).abs().max() / gw.abs().max())
+        err = float(torch.linalg.norm(p["gw"] - gw) / torch.linalg.norm(gw))
         assert err < 5e-2, (name, err)
