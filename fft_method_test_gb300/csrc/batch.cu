@@ -144,7 +144,9 @@ int tune(Problem& P, TuneResult* out) {
     for (int xr : xrows) {
         for (int xb = 0; xb < 2; ++xb) {
             for (int off = 0; off < 2; ++off) {
-                for (int lo = 0; lo < (off ? nlow : 1); ++lo) {
+                // lowreg: register-capped register-fed y/z passes, or the
+                // single-stage z pass of the specialised passes (TMA on)
+                for (int lo = 0; lo < nlow; ++lo) {
                     for (int t : tiles) {
                         apply_tiling(P, t, off != 0, xb == 0, xr, lo != 0);
                         double ms = 0.0;

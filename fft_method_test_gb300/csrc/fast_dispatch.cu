@@ -77,16 +77,21 @@ static cudaError_t fast_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     const CUtensorMap* smap = nullptr;
     const CUtensorMap* gmap = nullptr;
     if (!fast_maps(P, sizeof(T) == 8, TZ, &smap, &gmap)) return cudaErrorNotSupported;
-    const size_t zsmem = fast::z_smem_rt<T>(P.nz);
+    // the tuning flag of the register-capped y/z kernels selects here the
+    // single-stage z pass (three CTAs per SM instead of one two-stage CTA)
+    const int zstages = P.yz_lowreg ? 1 : 2;
+    const size_t zsmem = fast::z_smem_rt<T>(P.nz, zstages);
     const int ntz = (P.nxh + TZ - 1) / TZ;
     const int zgrid = (int)std::min<long long>(
-        (long long)ntz * P.ny, (long long)fast::z_blocks_per_sm<T>(P.nz, zsmem) * P.sm_count);
+        (long long)ntz * P.ny,
+        (long long)fast::z_blocks_per_sm<T>(P.nz, zstages, zsmem) * P.sm_count);
 
     cudaStream_t st = P.stream;
     cudaError_t e;
     if ((e = fast::run_xfwd<T>(P.nx, a, xgrid_f, xthreads, xsmem, st)) != cudaSuccess) return e;
     if ((e = fast::run_y<T>(P.ny, -1, a, ygrid, st)) != cudaSuccess) return e;
-    if ((e = fast::run_z<T>(P.nz, *smap, *gmap, a, dim3(zgrid), zsmem, st)) != cudaSuccess) return e;
+    if ((e = fast::run_z<T>(P.nz, zstages, *smap, *gmap, a, dim3(zgrid), zsmem, st)) != cudaSuccess)
+        return e;
     if ((e = fast::run_y<T>(P.ny, +1, a, ygrid, st)) != cudaSuccess) return e;
     if ((e = fast::run_xinv<T>(P.nx, a, stage_bytes, xgrid_i, xthreads, xismem, st)) != cudaSuccess)
         return e;

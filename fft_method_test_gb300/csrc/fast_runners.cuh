@@ -49,25 +49,35 @@ cudaError_t run_y(int n, int dir, const FastArgs& a, dim3 grid, cudaStream_t s) 
 }
 
 template <typename T>
-cudaError_t run_z(int n, const CUtensorMap& spec_map, const CUtensorMap& green_map, const FastArgs& a,
-                  dim3 grid, size_t smem, cudaStream_t s) {
+cudaError_t run_z(int n, int stages, const CUtensorMap& spec_map, const CUtensorMap& green_map,
+                  const FastArgs& a, dim3 grid, size_t smem, cudaStream_t s) {
     constexpr int TX = z_tx<T>();
-#define FP_CALL(N) FP_RUN((k_fz<T, N, TX>), grid, 3 * TX * Split<N>::R2, smem, s, spec_map, green_map, a)
+#define FP_CALL(N)                                                                                \
+    if (stages == 1)                                                                              \
+        FP_RUN((k_fz<T, N, TX, 1>), grid, 3 * TX * Split<N>::R2, smem, s, spec_map, green_map, a); \
+    else                                                                                          \
+        FP_RUN((k_fz<T, N, TX, 2>), grid, 3 * TX * Split<N>::R2, smem, s, spec_map, green_map, a)
     FP_FAST_SWITCH(n, FP_CALL)
 #undef FP_CALL
     return cudaGetLastError();
 }
 
 template <typename T>
-int z_blocks_per_sm(int n, size_t smem) {
+int z_blocks_per_sm(int n, int stages, size_t smem) {
     constexpr int TX = z_tx<T>();
     int nb = 0;
 #define FP_CALL(N)                                                                            \
     {                                                                                         \
-        static std::atomic<unsigned long long> f_{0};                                         \
-        ensure_max_smem(k_fz<T, N, TX>, f_);                                                  \
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fz<T, N, TX>,                    \
-                                                      3 * TX * Split<N>::R2, smem);           \
+        static std::atomic<unsigned long long> f1_{0}, f2_{0};                                \
+        if (stages == 1) {                                                                    \
+            ensure_max_smem(k_fz<T, N, TX, 1>, f1_);                                          \
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fz<T, N, TX, 1>,             \
+                                                          3 * TX * Split<N>::R2, smem);        \
+        } else {                                                                              \
+            ensure_max_smem(k_fz<T, N, TX, 2>, f2_);                                          \
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fz<T, N, TX, 2>,             \
+                                                          3 * TX * Split<N>::R2, smem);        \
+        }                                                                                     \
     }
     switch (n) {
         case 32: FP_CALL(32); break;
@@ -109,10 +119,10 @@ int x_blocks_per_sm(int n, bool inverse, int threads, size_t smem) {
     template cudaError_t run_xfwd<T>(int, const FastArgs&, int, int, size_t, cudaStream_t);         \
     template cudaError_t run_xinv<T>(int, const FastArgs&, int, int, int, size_t, cudaStream_t);    \
     template cudaError_t run_y<T>(int, int, const FastArgs&, dim3, cudaStream_t);                   \
-    template cudaError_t run_z<T>(int, const CUtensorMap&, const CUtensorMap&, const FastArgs&, dim3, \
-                                  size_t, cudaStream_t);                                            \
+    template cudaError_t run_z<T>(int, int, const CUtensorMap&, const CUtensorMap&, const FastArgs&, \
+                                  dim3, size_t, cudaStream_t);                                      \
     template int x_blocks_per_sm<T>(int, bool, int, size_t);                                      \
-    template int z_blocks_per_sm<T>(int, size_t);
+    template int z_blocks_per_sm<T>(int, int, size_t);
 
 }  // namespace fast
 }  // namespace fp

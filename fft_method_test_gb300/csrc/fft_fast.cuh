@@ -554,16 +554,18 @@ __host__ __device__ constexpr size_t z_stage_bytes() {
 }
 
 // Persistent CTAs walk the (kx tile, ky) tiles; thread = column + TX *
-// (owner + TPL * comp).  Two pipeline stages: while tile i is transformed,
-// one thread has the TMA engine bring the spectral tile (three boxes of
-// {2 TX reals, 1, nz}) and the Green tile (six boxes of {TX, 1, nz}) of tile
-// i + 1 into the other stage, completing on that stage's mbarrier.  Boxes
-// past the last kx column read zeros.  The phases that touch one component
-// only synchronise that component's threads (named barrier 1 + comp); the
-// Green multiply reads all three.  Waits are bounded: on a timeout the CTA
-// raises a.err and returns.
-template <typename T, int N, int TX>
-__global__ void __launch_bounds__(3 * TX * Split<N>::R2, 1)
+// (owner + TPL * comp).  One thread has the TMA engine bring the spectral
+// tile (three boxes of {2 TX reals, 1, nz}) and the Green tile (six boxes of
+// {TX, 1, nz}) into a stage, completing on that stage's mbarrier; boxes past
+// the last kx column read zeros.  With two stages the tiles of iteration
+// i + 1 load while tile i is transformed (one CTA per SM); with one stage the
+// next tile loads after the current one is done, and three CTAs per SM (at
+// most 112 registers per thread) overlap one another instead.  The phases
+// that touch one component only synchronise that component's threads (named
+// barrier 1 + comp); the Green multiply reads all three.  Waits are bounded:
+// on a timeout the CTA raises a.err and returns.
+template <typename T, int N, int TX, int STAGES>
+__global__ void __launch_bounds__(3 * TX * Split<N>::R2, STAGES == 1 ? 3 : 1)
     k_fz(const __grid_constant__ CUtensorMap spec_map, const __grid_constant__ CUtensorMap green_map,
          FastArgs a) {
     if (a.skip && *a.skip) return;
@@ -608,13 +610,21 @@ __global__ void __launch_bounds__(3 * TX * Split<N>::R2, 1)
     long long tile = blockIdx.x;
     if (threadIdx.x == 0 && tile < ntiles) issue(tile, 0);
     for (int i = 0; tile < ntiles; tile += gridDim.x, ++i) {
-        const int st = i & 1;
+        const int st = STAGES == 2 ? (i & 1) : 0;
         const long long next = tile + gridDim.x;
-        if (threadIdx.x == 0 && next < ntiles) {
-            fence_proxy_async_smem();
-            issue(next, st ^ 1);
+        if (STAGES == 2) {
+            if (threadIdx.x == 0 && next < ntiles) {
+                fence_proxy_async_smem();
+                issue(next, st ^ 1);
+            }
+            if (!tma_pipeline_wait<T2>(bars, i, st, next < ntiles, a.err)) return;
+        } else {
+            const bool ok = mbar_wait_bounded(&bars[0], (uint32_t)(i & 1));
+            if (__syncthreads_or(!ok)) {
+                if (threadIdx.x == 0) atomicExch(a.err, 1);
+                return;
+            }
         }
-        if (!tma_pipeline_wait<T2>(bars, i, st, next < ntiles, a.err)) return;
         T2* blk = reinterpret_cast<T2*>(stage0 + st * STAGE);
         const T* gsm = reinterpret_cast<const T*>(stage0 + st * STAGE + GOFF);
         const int k0 = (int)(tile % ntx) * TX;
@@ -658,7 +668,11 @@ __global__ void __launch_bounds__(3 * TX * Split<N>::R2, 1)
             auto st_g = [&](int pos, T2 v) { base[pos * es] = v; };
             stage_b<R2, R1, +1, TPL, false>(my, t, act, st_g);
         }
-        __syncthreads();  // this stage is refilled by the issue of iteration i + 1
+        __syncthreads();  // this stage is refilled by the next issue
+        if (STAGES == 1 && threadIdx.x == 0 && next < ntiles) {
+            fence_proxy_async_smem();
+            issue(next, 0);
+        }
     }
 }
 
@@ -718,15 +732,15 @@ int x_ld_rt(int n) {
     }
 }
 
-// dynamic shared memory of the z pass: mbarriers + two pipeline stages
+// dynamic shared memory of the z pass: mbarriers + its pipeline stages
 template <typename T>
-size_t z_smem_rt(int n) {
+size_t z_smem_rt(int n, int stages) {
     constexpr int TX = z_tx<T>();
     switch (n) {
-        case 32: return 128 + 2 * z_stage_bytes<T, 32, TX>();
-        case 64: return 128 + 2 * z_stage_bytes<T, 64, TX>();
-        case 128: return 128 + 2 * z_stage_bytes<T, 128, TX>();
-        default: return 128 + 2 * z_stage_bytes<T, 256, TX>();
+        case 32: return 128 + stages * z_stage_bytes<T, 32, TX>();
+        case 64: return 128 + stages * z_stage_bytes<T, 64, TX>();
+        case 128: return 128 + stages * z_stage_bytes<T, 128, TX>();
+        default: return 128 + stages * z_stage_bytes<T, 256, TX>();
     }
 }
 
@@ -738,11 +752,11 @@ cudaError_t run_xinv(int n, const FastArgs& a, int stage_bytes, int grid, int th
 template <typename T>
 cudaError_t run_y(int n, int dir, const FastArgs& a, dim3 grid, cudaStream_t s);
 template <typename T>
-cudaError_t run_z(int n, const CUtensorMap& spec_map, const CUtensorMap& green_map, const FastArgs& a,
-                  dim3 grid, size_t smem, cudaStream_t s);
+cudaError_t run_z(int n, int stages, const CUtensorMap& spec_map, const CUtensorMap& green_map,
+                  const FastArgs& a, dim3 grid, size_t smem, cudaStream_t s);
 // blocks of the z kernel resident per SM at this shared-memory size
 template <typename T>
-int z_blocks_per_sm(int n, size_t smem);
+int z_blocks_per_sm(int n, int stages, size_t smem);
 
 // blocks of the x kernels resident per SM at this shared-memory size
 template <typename T>
