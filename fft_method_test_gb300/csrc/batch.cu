@@ -185,6 +185,13 @@ struct Job {
 }  // namespace
 }  // namespace fp
 
+extern "C" int fp_time_apply(fp_handle h, int reps, double* ms) {
+    if (!h || reps <= 0 || !ms) return FP_ERR_INVALID;
+    const int rc = fp::time_apply(h->P, reps, ms);
+    if (rc != FP_OK) h->P.err = "fp_time_apply: an operator apply failed";
+    return rc;
+}
+
 extern "C" int fp_autotune(fp_handle h, int* tile, int* tma_off, int* x_bulk, int* x_rows,
                            int* lowreg, double* apply_ms) {
     using namespace fp;

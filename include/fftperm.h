@@ -178,6 +178,11 @@ int fp_write_fvel(const char* path, int nx, int ny, int nz, double porosity, dou
  * to rounding).  Outputs may be NULL. */
 int fp_autotune(fp_handle h, int* tile, int* tma_off, int* x_bulk, int* x_rows, int* lowreg,
                 double* apply_ms);
+/* A diagnostic with no counterpart in the reference: the mean CUDA-event
+ * time (ms) of `reps` back-to-back operator applies as MINRES runs them (the
+ * five FFT passes with the scatter and gather fused, on the handle's compact
+ * vectors, current precision and tiling), after one warm-up apply. */
+int fp_time_apply(fp_handle h, int reps, double* ms);
 /* Sets a tiling directly (for example one fp_autotune reported earlier):
  * tile in {0 = default, 2, 4, 8, 16, 32}, tma_off != 0 for the register-fed
  * y/z passes, x_bulk != 0 for the bulk-copy inverse x pass, x_rows > 0 caps
