@@ -61,11 +61,12 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--mode", default="solve",
-                    choices=["solve", "apply", "batch", "learned", "brinkman"],
+                    choices=["solve", "apply", "batch", "learned", "brinkman", "pradius", "rve"],
                     help="solve: the headline (seconds to K at 256^3); apply: --reps operator "
                          "applies per precision (for profilers); batch: 64 uneven "
                          "microstructures; brinkman: the C2 Brinkman cell; learned: the "
-                         "learned warm start")
+                         "learned warm start; pradius: K against the Green alias radius; "
+                         "rve: RVE-size sweep on the batched engine")
     ap.add_argument("--precision", default="mixed,fp64", help="precisions for --mode apply")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--tiling", default="",
@@ -745,6 +746,70 @@ def run_learned(args):
     print(json.dumps(line), flush=True)
 
 
+def run_pradius(args):
+    """Convergence of K with the alias radius P of the energy-consistent Green
+    sum (the reference fixes P = 2 and leaves the study open,
+    GreenOperator.cpp:98): FP64, tol 1e-10, P = 0..4, on the C1 cell (32^3
+    spheres r 4, porosity 0.6, seed 1001) and a 64^3 Gaussian field (l 6,
+    porosity 0.35, seed 3064).  Reports K and its relative change against
+    the largest P."""
+    from fft_method_test_gb300 import geometry as G
+    from fft_method_test_gb300.permeability import PermeabilityProblem
+
+    cells = {"c1_spheres32": G.spheres(32, 4.0, 0.60, seed=1001),
+             "grf64_phi0.35_l6_seed3064": G.gaussian_field(64, 6.0, 0.35, seed=3064)}
+    radii = [0, 1, 2, 3, 4]
+    out = {}
+    for name, m in cells.items():
+        Ks = {}
+        for pr in radii:
+            t0 = time.perf_counter()
+            with PermeabilityProblem(m.shape, precision="fp64", p_radius=pr) as p:
+                p.set_geometry(m)
+                K, st = p.solve_permeability(TOL_FP64, MAXIT)
+            Ks[pr] = (K, time.perf_counter() - t0, [s["iterations"] for s in st])
+        Kref = Ks[radii[-1]][0]
+        out[name] = {str(pr): {"K": np.asarray(K).tolist(), "seconds": t, "iterations": its,
+                               "K_rel_diff_vs_P%d" % radii[-1]:
+                                   float(np.linalg.norm(K - Kref) / np.linalg.norm(Kref))}
+                     for pr, (K, t, its) in Ks.items()}
+    print(json.dumps({"metric": "green_alias_radius_study", "data": "synthetic", "n_gpus": 1,
+                      "precision": "fp64", "tol": TOL_FP64, "cells": out}), flush=True)
+
+
+def run_rve(args):
+    """RVE-size sweep on the batched engine: Gaussian random fields (l 6,
+    porosity 0.35) of edges 32, 48, 64, 96 and 128, eight independent
+    realisations per edge (seeds 40000 + 100 * edge + k), solved together by
+    fp_batch_solve_permeability (mixed, tol 1e-7).  Reports per edge the mean
+    and standard deviation of the diagonal of K and of its mean, the measure
+    of how far a cell of that edge is from representative."""
+    from fft_method_test_gb300 import geometry as G
+    from fft_method_test_gb300.permeability import batch_solve_permeability
+
+    edges = [32, 48, 64, 96, 128]
+    reals = 8
+    masks, owner = [], []
+    for e in edges:
+        for k in range(reals):
+            masks.append(G.gaussian_field(e, 6.0, 0.35, seed=40000 + 100 * e + k))
+            owner.append(e)
+    t0 = time.perf_counter()
+    K, st, status = batch_solve_permeability(masks, precision="mixed", tol=TOL_MIXED, maxit=MAXIT,
+                                             concurrency=args.concurrency, autotune=True)
+    dt = time.perf_counter() - t0
+    res = {}
+    for e in edges:
+        ks = np.array([np.trace(K[i]) / 3.0 for i in range(len(masks)) if owner[i] == e])
+        diag = np.array([np.diag(K[i]) for i in range(len(masks)) if owner[i] == e])
+        res[str(e)] = {"realisations": int(len(ks)), "mean_K": float(ks.mean()),
+                       "std_K": float(ks.std(ddof=1)), "rel_std": float(ks.std(ddof=1) / ks.mean()),
+                       "mean_diag": diag.mean(axis=0).tolist()}
+    print(json.dumps({"metric": "rve_size_sweep", "data": "synthetic", "n_gpus": 1,
+                      "precision": "mixed", "tol": TOL_MIXED, "seconds": dt,
+                      "all_ok": bool(all(c == 0 for c in status)), "edges": res}), flush=True)
+
+
 def run_brinkman(args):
     """C2: Brinkman penalisation on a 128^3 cell of radius-8 spheres at
     porosity 0.45 (seed 1002), penalty 1e4, viscosity 1, unit force along x.
@@ -846,6 +911,12 @@ def main():
         return
     if args.mode == "batch":
         run_batch(args)
+        return
+    if args.mode == "pradius":
+        run_pradius(args)
+        return
+    if args.mode == "rve":
+        run_rve(args)
         return
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
