@@ -41,6 +41,7 @@ EXPORTED = [
     "fp_nn_conv", "fp_nn_wgrad", "fp_nn_bias_grad", "fp_nn_relu_back", "fp_nn_adam", "fp_nn_loss",
     "fp_measure_fp64_rate", "fp_nn_conv_tc", "fp_nn_tc_error", "fp_nn_pool2", "fp_nn_pool2_back",
     "fp_nn_up2_add", "fp_nn_up2_add_back", "fp_nn_wgrad_cc", "fp_time_apply",
+    "fp_load_fgeo", "fp_recover_fvel",
 ]
 
 
@@ -91,6 +92,8 @@ _SIGNATURES = {
     "fp_kernel_launch_count": ([], C.c_longlong),
     "fp_measure_fp64_rate": ([C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
     "fp_time_apply": ([C.c_void_p, C.c_int, C.POINTER(C.c_double)], C.c_int),
+    "fp_load_fgeo": ([C.c_void_p, C.c_char_p, C.c_uint32, C.c_int, C.POINTER(C.c_int64)], C.c_int),
+    "fp_recover_fvel": ([C.c_void_p, C.c_char_p, _dp, _dp, C.c_double, C.c_double], C.c_int),
     "fp_set_precision": ([_h, C.c_int], C.c_int),
     "fp_set_geometry": ([_h, _u8p, C.c_int, C.POINTER(C.c_int64)], C.c_int),
     "fp_get_support": ([_h, _i64p], C.c_int),

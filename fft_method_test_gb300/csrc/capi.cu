@@ -6,6 +6,7 @@
 // vector on the device between the copies.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -413,6 +414,8 @@ int device_recover(Problem& P, const double g[3], const double* d_x, double avg[
     return FP_OK;
 }
 
+int finish_geometry(Problem& P, int64_t* nb_out);
+
 double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
         .count();
@@ -567,6 +570,105 @@ int fp_set_geometry(fp_handle h, const uint8_t* fluid_mask, int support_mode, in
     P.support_mode = support_mode;
     FP_CUDA(cudaMemcpyAsync(P.d_mask, fluid_mask, (size_t)P.n, cudaMemcpyHostToDevice, P.stream),
             "mask copy");
+    return finish_geometry(P, nb_out);
+}
+
+int fp_load_fgeo(fp_handle h, const char* path, uint32_t fluid_id, int support_mode,
+                 int64_t* nb_out) {
+    if (!h) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    if (!path) return fail(P, FP_ERR_INVALID, "VoxelIO: path must not be null");
+    if (support_mode != FP_SUPPORT_INTERFACE && support_mode != FP_SUPPORT_FULLSOLID)
+        return fail(P, FP_ERR_INVALID, "unknown support mode");
+    std::FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(P, FP_ERR_INVALID, std::string("VoxelIO: cannot open ") + path);
+    unsigned char head[32];
+    const bool got = std::fread(head, 1, 32, f) == 32;
+    if (!got || std::memcmp(head, "FGEO", 4) != 0) {
+        std::fclose(f);
+        return fail(P, FP_ERR_INVALID, std::string("VoxelIO: invalid .fgeo magic: ") + path);
+    }
+    if (head[4] != 1 || (head[5] != 1 && head[5] != 2)) {
+        std::fclose(f);
+        return fail(P, FP_ERR_INVALID, "VoxelIO: unsupported .fgeo version or value type");
+    }
+    uint64_t dims[3];
+    std::memcpy(dims, head + 8, 24);
+    if (dims[0] != (uint64_t)P.nx || dims[1] != (uint64_t)P.ny || dims[2] != (uint64_t)P.nz) {
+        std::fclose(f);
+        return fail(P, FP_ERR_INVALID, "VoxelIO: .fgeo dimensions differ from the grid");
+    }
+    const int esz = head[5] == 1 ? 4 : 2;
+    free_geometry(P);
+    P.support_mode = support_mode;
+    // the ids stream to the device in chunks; the mask is formed there
+    const long long chunk = 1LL << 24;
+    void* d_ids = nullptr;
+    {
+        const cudaError_t e = dalloc(P, reinterpret_cast<unsigned char**>(&d_ids),
+                                     (size_t)std::min<long long>(chunk, P.n) * esz);
+        if (e != cudaSuccess) {
+            std::fclose(f);
+            return cuda_fail(P, e, "cudaMalloc ids");
+        }
+    }
+    std::vector<unsigned char> host((size_t)std::min<long long>(chunk, P.n) * esz);
+    int rc = FP_OK;
+    for (long long i0 = 0; i0 < P.n && rc == FP_OK; i0 += chunk) {
+        const long long m = std::min<long long>(chunk, P.n - i0);
+        if (std::fread(host.data(), esz, (size_t)m, f) != (size_t)m) {
+            rc = fail(P, FP_ERR_INVALID, "VoxelIO: .fgeo payload is truncated");
+            break;
+        }
+        cudaError_t e = cudaMemcpyAsync(d_ids, host.data(), (size_t)m * esz, cudaMemcpyHostToDevice,
+                                        P.stream);
+        if (e == cudaSuccess) e = fp::launch_ids_to_mask(d_ids, esz, m, fluid_id, P.d_mask + i0, P.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(P.stream);  // host buffer reused
+        if (e != cudaSuccess) rc = cuda_fail(P, e, "ids to mask");
+    }
+    std::fclose(f);
+    dfree(P, d_ids);
+    if (rc != FP_OK) return rc;
+    return finish_geometry(P, nb_out);
+}
+
+int fp_recover_fvel(fp_handle h, const char* path, const double grad[3], const double* x,
+                    double porosity, double viscosity) {
+    if (!h || !path || !grad || !x) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    int rc = need_geometry(P, "VelocityRecovery::recover");
+    if (rc) return rc;
+    const size_t m = 3 * (size_t)P.nb;
+    FP_CUDA(cudaMemcpyAsync(P.d_cin, x, sizeof(double) * m, cudaMemcpyHostToDevice, P.stream), "copy");
+    double avg[3];
+    rc = device_recover(P, grad, P.d_cin, avg, true);
+    if (rc) return rc;
+    std::FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(P, FP_ERR_INVALID, std::string("cannot write velocity file: ") + path);
+    bool ok = fp::write_fvel_header(f, P.nx, P.ny, P.nz, porosity, viscosity, grad);
+    // the field leaves the device one chunk per component at a time
+    const long long chunk = 1LL << 20;
+    std::vector<double> comp(3 * (size_t)std::min<long long>(chunk, P.n)), rec(comp.size());
+    for (long long i0 = 0; ok && i0 < P.n; i0 += chunk) {
+        const long long k = std::min<long long>(chunk, P.n - i0);
+        for (int c = 0; c < 3; ++c)
+            FP_CUDA(cudaMemcpyAsync(comp.data() + (size_t)c * k, P.d_dense_out + (size_t)c * P.n + i0,
+                                    sizeof(double) * k, cudaMemcpyDeviceToHost, P.stream),
+                    "copy");
+        FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+        for (long long i = 0; i < k; ++i)
+            for (int c = 0; c < 3; ++c) rec[3 * i + c] = comp[(size_t)c * k + i];
+        ok = std::fwrite(rec.data(), sizeof(double), 3 * (size_t)k, f) == 3 * (size_t)k;
+    }
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? FP_OK : fail(P, FP_ERR_INVALID, std::string("cannot write velocity file: ") + path);
+}
+
+}  // extern "C"
+
+namespace {
+
+int finish_geometry(Problem& P, int64_t* nb_out) {
     FP_CUDA(fp::launch_support(P), "support");
     const size_t m = 3 * (size_t)P.nb;
     FP_CUDA(dalloc(P, &P.d_cin, m), "cudaMalloc");
@@ -583,6 +685,10 @@ int fp_set_geometry(fp_handle h, const uint8_t* fluid_mask, int support_mode, in
     if (nb_out) *nb_out = P.nb;
     return FP_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 int fp_get_support(fp_handle h, int64_t* out) {
     if (!h || !out) return FP_ERR_INVALID;

@@ -178,6 +178,13 @@ cudaError_t launch_green_kernel(const GreenArgs& a, cudaStream_t stream);
 // not factor into 2, 3 and 5 or exceeds the supported maximum.
 bool fill_plan_radices(int n, FftPlanDev& d);
 cudaError_t launch_support(Problem& P);
+// mask[i] = (ids[i] == fluid_id) for `count` material ids of 2 or 4 bytes
+cudaError_t launch_ids_to_mask(const void* ids, int id_bytes, long long count, uint32_t fluid_id,
+                               uint8_t* mask, cudaStream_t stream);
+// The .fvel header (io.cu): "FVEL", version 1, dims, porosity, viscosity,
+// driving gradient; false when it cannot be written.
+bool write_fvel_header(void* file, int nx, int ny, int nz, double porosity, double viscosity,
+                       const double driving[3]);
 // Computes the Green table into g64 and/or g32 (either may be null).
 cudaError_t launch_green(Problem& P, double* g64, float* g32);
 

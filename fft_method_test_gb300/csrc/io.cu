@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/fftperm.h"
+#include "internal.h"
 
 namespace {
 
@@ -23,14 +24,9 @@ bool little_endian() {
 
 }  // namespace
 
-extern "C" int fp_write_fvel(const char* path, int nx, int ny, int nz, double porosity,
-                             double viscosity, const double driving[3], const double* vx,
-                             const double* vy, const double* vz) {
-    if (!path || nx <= 0 || ny <= 0 || nz <= 0 || !driving || !vx || !vy || !vz)
-        return FP_ERR_INVALID;
-    if (!little_endian()) return FP_ERR_UNSUPPORTED;  // the format is little-endian
-    std::FILE* f = std::fopen(path, "wb");
-    if (!f) return FP_ERR_INVALID;
+namespace fp {
+bool write_fvel_header(void* file, int nx, int ny, int nz, double porosity, double viscosity,
+                       const double driving[3]) {
     unsigned char head[72];
     std::memset(head, 0, sizeof(head));
     std::memcpy(head, "FVEL", 4);
@@ -40,7 +36,19 @@ extern "C" int fp_write_fvel(const char* path, int nx, int ny, int nz, double po
     std::memcpy(head + 32, &porosity, 8);
     std::memcpy(head + 40, &viscosity, 8);
     std::memcpy(head + 48, driving, 24);
-    bool ok = std::fwrite(head, 1, sizeof(head), f) == sizeof(head);
+    return std::fwrite(head, 1, sizeof(head), static_cast<std::FILE*>(file)) == sizeof(head);
+}
+}  // namespace fp
+
+extern "C" int fp_write_fvel(const char* path, int nx, int ny, int nz, double porosity,
+                             double viscosity, const double driving[3], const double* vx,
+                             const double* vy, const double* vz) {
+    if (!path || nx <= 0 || ny <= 0 || nz <= 0 || !driving || !vx || !vy || !vz)
+        return FP_ERR_INVALID;
+    if (!little_endian()) return FP_ERR_UNSUPPORTED;  // the format is little-endian
+    std::FILE* f = std::fopen(path, "wb");
+    if (!f) return FP_ERR_INVALID;
+    bool ok = fp::write_fvel_header(f, nx, ny, nz, porosity, viscosity, driving);
     const size_t n = (size_t)nx * ny * nz;
     const size_t chunk = 1 << 16;
     std::vector<double> rec(3 * chunk);

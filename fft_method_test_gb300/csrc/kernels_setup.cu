@@ -122,6 +122,30 @@ __global__ void k_support_write(const uint8_t* __restrict__ mask, int nx, int ny
     }
 }
 
+// mask[i] = (ids[i] == fluid_id) for one chunk of material ids (u16 or u32)
+template <typename I>
+__global__ void k_ids_to_mask(const I* __restrict__ ids, long long count, uint32_t fluid_id,
+                              uint8_t* __restrict__ mask) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (long long)gridDim.x * blockDim.x)
+        mask[i] = (uint32_t)ids[i] == fluid_id ? 1 : 0;
+}
+
+cudaError_t launch_ids_to_mask(const void* ids, int id_bytes, long long count, uint32_t fluid_id,
+                               uint8_t* mask, cudaStream_t stream) {
+    long long blocks = (count + 255) / 256;
+    if (blocks > 65535LL * 8) blocks = 65535LL * 8;
+    if (blocks < 1) blocks = 1;
+    FP_LAUNCHED();
+    if (id_bytes == 2)
+        k_ids_to_mask<uint16_t><<<(unsigned)blocks, 256, 0, stream>>>(
+            static_cast<const uint16_t*>(ids), count, fluid_id, mask);
+    else
+        k_ids_to_mask<uint32_t><<<(unsigned)blocks, 256, 0, stream>>>(
+            static_cast<const uint32_t*>(ids), count, fluid_id, mask);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_support(Problem& P) {
     const int threads = 256;
     const long long warps = P.nrows;

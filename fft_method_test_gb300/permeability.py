@@ -125,6 +125,25 @@ class PermeabilityProblem:
         self.mask = m
         return self.nb
 
+    def load_fgeo(self, path: str, fluid_id: int = 1, support: str = "interface") -> int:
+        """fp_load_fgeo: the geometry of a .fgeo file, the mask formed on the device."""
+        if support not in SUPPORT_MODES:
+            raise ValueError("unknown support mode " + repr(support))
+        nb = C.c_int64(0)
+        self._check(self.lib.fp_load_fgeo(self._h, path.encode(), int(fluid_id),
+                                          SUPPORT_MODES[support], C.byref(nb)))
+        self.nb = int(nb.value)
+        self.mask = None
+        return self.nb
+
+    def recover_fvel(self, path: str, grad, x, porosity: float, viscosity: float = 1.0) -> None:
+        """fp_recover_fvel: the recovered velocity field written to a .fvel file."""
+        x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+        if x.size != 3 * self.nb:
+            raise ValueError("VelocityRecovery::recover compact solution size mismatch")
+        self._check(self.lib.fp_recover_fvel(self._h, path.encode(), np.asarray(grad, np.float64), x,
+                                             float(porosity), float(viscosity)))
+
     def support(self) -> np.ndarray:
         out = np.zeros(max(self.nb, 1), dtype=np.int64)
         self._check(self.lib.fp_get_support(self._h, out))

@@ -86,6 +86,13 @@ int fp_set_precision(fp_handle h, int precision);
  * src/bignonnet/ForceSupport.cpp:9-25, src/geometry/InterfaceVoxels.cpp:7-43).
  * fluid_mask has N bytes.  *nb_out receives N_B (may be NULL). */
 int fp_set_geometry(fp_handle h, const uint8_t* fluid_mask, int support_mode, int64_t* nb_out);
+/* VoxelIO::load_fgeo + BinaryMedium + ForceSupport (src/io/VoxelIO.cpp:89-159):
+ * reads the reference's binary .fgeo file (magic "FGEO", version 1, value
+ * type 1 = u32 or 2 = u16, 2 reserved bytes, nx ny nz as little-endian u64,
+ * then one id per voxel, x fastest), streams the ids to the device in chunks
+ * and forms the fluid mask there (id == fluid_id), then the support set as
+ * fp_set_geometry.  The file's dimensions must be the handle's. */
+int fp_load_fgeo(fp_handle h, const char* path, uint32_t fluid_id, int support_mode, int64_t* nb_out);
 /* ForceSupport::active_voxels (src/bignonnet/ForceSupport.hpp:22): N_B ascending flat indices. */
 int fp_get_support(fp_handle h, int64_t* out);
 /* Symmetrised Green tensor on the half spectrum, 6 blocks (xx xy xz yy yz zz)
@@ -159,6 +166,12 @@ int fp_solve_permeability(fp_handle h, double tol, int64_t maxit, double K[9],
 int fp_green_apply_noalloc(int nx, int ny, int nz, double voxel_size, double mu, int p_radius,
                            const double* d_force_soa, double* d_velocity_soa, void* stream);
 
+/* fp_recover followed by the reference's .fvel file of the recovered field
+ * (write_velocity_field_binary, src/app/PermeabilityRunner.cpp:109-159): the
+ * field is formed on the device and leaves it in chunks straight into the
+ * file; driving = grad.  x: 3*N_B compact interface forces (host). */
+int fp_recover_fvel(fp_handle h, const char* path, const double grad[3], const double* x,
+                    double porosity, double viscosity);
 /* The reference's .fvel velocity file (write_velocity_field_binary,
  * src/app/PermeabilityRunner.cpp:109-159) from SoA host fields of N doubles
  * each (for example the field of fp_recover).  FP_ERR_INVALID when the file

@@ -148,3 +148,53 @@ def test_golden_green_3x5x6_direct(gpu_lib):
     with problem((nz, ny, nx)) as p:
         got = p.green_tensor()
     assert rel_err(got, want) < 1e-13
+
+
+def test_fgeo_ingested_on_device_matches_host_mask(gpu_lib, tmp_path):
+    """fp_load_fgeo (the reference's .fgeo read, the mask formed on the device
+    from u16 and u32 ids) gives the support set of fp_set_geometry on the
+    same mask, and a wrong size or magic is an argument error."""
+    from fft_method_test_gb300._capi import FpError
+
+    mask = G.gaussian_field((24, 20, 16), 3.0, 0.4, seed=77)
+    ids16 = np.where(mask != 0, 1, 2).astype(np.uint16)
+    f16 = tmp_path / "g16.fgeo"
+    G.write_fgeo(str(f16), ids16, ids=True)
+    f32 = tmp_path / "g32.fgeo"
+    nz, ny, nx = mask.shape
+    with open(f32, "wb") as fh:
+        fh.write(b"FGEO" + bytes([1, 1, 0, 0]))
+        fh.write(np.array([nx, ny, nz], "<u8").tobytes())
+        fh.write(np.where(mask != 0, 7, 3).astype("<u4").tobytes())
+    with problem(mask.shape) as p:
+        nb = p.set_geometry(mask)
+        want = p.support()
+        assert p.load_fgeo(str(f16), fluid_id=1) == nb
+        assert np.array_equal(p.support(), want)
+        assert p.load_fgeo(str(f32), fluid_id=7) == nb
+        assert np.array_equal(p.support(), want)
+    bad = tmp_path / "bad.fgeo"
+    bad.write_bytes(b"NOPE" + bytes(28))
+    with problem((8, 8, 8)) as p:
+        with pytest.raises((ValueError, FpError)):
+            p.load_fgeo(str(f16))  # dimensions differ from the grid
+        with pytest.raises((ValueError, FpError)):
+            p.load_fgeo(str(bad))
+
+
+def test_velocity_file_written_from_device(gpu_lib, tmp_path):
+    """fp_recover_fvel writes the recovered field in the reference's .fvel
+    layout, equal to fp_recover's field."""
+    from fft_method_test_gb300.permeability import read_fvel
+
+    mask = G.spheres(16, 3.0, 0.6, seed=7)
+    with problem(mask.shape) as p:
+        nb = p.set_geometry(mask)
+        x = np.random.default_rng(1).uniform(-1, 1, 3 * nb)
+        _, v = p.recover((1.0, 0.0, 0.0), x, want_field=True)
+        path = tmp_path / "v.fvel"
+        p.recover_fvel(str(path), (1.0, 0.0, 0.0), x, porosity=0.6, viscosity=1.0)
+    d = read_fvel(str(path))
+    assert d["velocity"].shape == v.shape
+    assert np.array_equal(d["velocity"], v)
+    assert d["porosity"] == 0.6 and np.array_equal(d["driving"], [1.0, 0.0, 0.0])
