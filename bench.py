@@ -61,12 +61,14 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--mode", default="solve",
-                    choices=["solve", "apply", "batch", "learned", "brinkman", "pradius", "rve"],
+                    choices=["solve", "apply", "batch", "learned", "brinkman", "pradius", "rve",
+                             "unet"],
                     help="solve: the headline (seconds to K at 256^3); apply: --reps operator "
                          "applies per precision (for profilers); batch: 64 uneven "
                          "microstructures; brinkman: the C2 Brinkman cell; learned: the "
                          "learned warm start; pradius: K against the Green alias radius; "
-                         "rve: RVE-size sweep on the batched engine")
+                         "rve: RVE-size sweep on the batched engine; unet: U-Net forward "
+                         "passes (for profilers)")
     ap.add_argument("--precision", default="mixed,fp64", help="precisions for --mode apply")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--tiling", default="",
@@ -746,6 +748,24 @@ def run_learned(args):
     print(json.dumps(line), flush=True)
 
 
+def run_unet_forward(args):
+    """Profiling entry: the warm-start U-Net's forward pass (tcgen05
+    convolutions) on a batch of four 64^3 sphere packings, --reps times."""
+    import torch
+
+    from fft_method_test_gb300 import geometry as G
+    from fft_method_test_gb300 import learned as L
+
+    net = L.UNetWarmStart(seed=0)
+    masks = [G.spheres(64, 5.0, 0.5, seed=k) for k in range(4)]
+    m = torch.tensor(np.concatenate([x.ravel() for x in masks]), device="cuda")
+    feat = L.features_gpu(m, (m == 0).to(torch.uint8))
+    for _ in range(args.reps):
+        out, _ = net.forward(feat, (64, 64, 64), 4)
+    torch.cuda.synchronize()
+    print("unet forward done", float(out.abs().sum()), flush=True)
+
+
 def run_pradius(args):
     """Convergence of K with the alias radius P of the energy-consistent Green
     sum (the reference fixes P = 2 and leaves the study open,
@@ -911,6 +931,9 @@ def main():
         return
     if args.mode == "batch":
         run_batch(args)
+        return
+    if args.mode == "unet":
+        run_unet_forward(args)
         return
     if args.mode == "pradius":
         run_pradius(args)
