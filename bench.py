@@ -887,8 +887,20 @@ def run_brinkman(args):
     t0 = time.perf_counter()
     K_br, st_br = computePermeabilityTensorFixedPoint(ids, solid_penalty=1e4, tolerance=1e-8)
     t_brk = time.perf_counter() - t0
+    # both methods on a plate channel, where the continuum answer is known:
+    # solid slab z < 8 in a 64^3 cell, fluid gap g = 56, flow along x;
+    # superficial K_xx = porosity * g^2 / 12 (plane Poiseuille flow)
+    ch = np.ones((64, 64, 64), np.uint8)
+    ch[:8] = 0
+    with PermeabilityProblem(ch.shape, precision="fp64") as pv:
+        pv.set_geometry(ch)
+        K_ch_var, _ = pv.solve_permeability(TOL_FP64, MAXIT)
+    K_ch_br, _ = computePermeabilityTensorFixedPoint(G.to_ids(ch), solid_penalty=1e4, tolerance=1e-8)
+    channel = {"analytic_Kxx": float(56.0 / 64.0 * 56.0 ** 2 / 12.0),
+               "variational_Kxx": float(K_ch_var[0, 0]), "brinkman_Kxx": float(K_ch_br[0, 0])}
     fx = oracle_fixture("c2_128_sph", mask)
     comparison = {
+        "plate_channel_64": channel,
         "variational": {"K": np.asarray(K_var).tolist(), "tol": TOL_FP64, "seconds": t_var,
                         "iterations": [s["iterations"] for s in st_var],
                         "K_rel_err_vs_oracle": (float(np.linalg.norm(K_var - fx["K"]) /
