@@ -473,6 +473,10 @@ int fp::create_handle(int nx, int ny, int nz, double voxel_size, double mu, int 
     }
     if (const char* t = std::getenv("FFTPERM_NO_GRAPHS")) P.use_graphs = std::atoi(t) == 0;
     if (const char* t = std::getenv("FFTPERM_NO_FAST")) P.fast_off = std::atoi(t) != 0;
+    if (const char* t = std::getenv("FFTPERM_RELIABLE")) {
+        const int k = std::atoi(t);
+        if (k > 0) P.reliable_interval = k;
+    }
     if (const char* t = std::getenv("FFTPERM_AHEAD")) {
         const double f = std::atof(t);
         if (f > 0.0 && f < 1.0) P.ahead_factor = f;
@@ -489,6 +493,7 @@ int fp::create_handle(int nx, int ny, int nz, double voxel_size, double mu, int 
     const size_t nparts = (size_t)std::max<long long>(fp::kMaxPartials, P.nrows + 64);
     FP_CUDA(dalloc(P, &P.d_partials, 4 * nparts), "cudaMalloc partials");
     FP_CUDA(dalloc(P, &P.d_red, 64), "cudaMalloc red");
+    FP_CUDA(cudaMemsetAsync(P.d_red, 0, sizeof(double) * 64, P.stream), "memset red");
     FP_CUDA(dalloc(P, &P.d_sc, 1), "cudaMalloc scalars");
     FP_CUDA(dalloc(P, &P.d_err, 1), "cudaMalloc error flag");
     FP_CUDA(cudaMemsetAsync(P.d_err, 0, sizeof(int), P.stream), "memset");

@@ -155,6 +155,9 @@ struct Problem {
 };
 
 constexpr int kMaxPartials = 8192;
+// d_red slot (in doubles) holding the block-count tickets of the fused MINRES
+// vector kernels (two unsigned ints, zero between launches)
+constexpr int kTicketSlot = 56;
 
 // ---- setup kernels (kernels_setup.cu) ----
 // Inputs of the Green-table kernel: per-axis tables of sinc(pi m / n) and

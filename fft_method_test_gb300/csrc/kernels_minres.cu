@@ -102,11 +102,18 @@ __global__ void k_alpha(MinresScalars* sc, const double* __restrict__ partials, 
     }
 }
 
+__device__ void scalar_step(MinresScalars* sc, const double* __restrict__ partials, int nparts,
+                            double* hist, double* red);
+__device__ void finish_step(MinresScalars* sc, const double* __restrict__ partials, int nparts,
+                            double* red);
+__device__ __forceinline__ bool last_block(unsigned int* counter);
+
 // Two voxels (six doubles, three aligned double2) per thread: components are
 // static, loads are 16-byte vectors.  The odd tail voxel is handled by the
 // first thread of block 0.
-__global__ void k_zupd(const MinresScalars* sc, double* __restrict__ z, const double* __restrict__ v,
-                       const double* __restrict__ v_old, long long nb, double* partials) {
+__global__ void k_zupd(MinresScalars* sc, double* __restrict__ z, const double* __restrict__ v,
+                       const double* __restrict__ v_old, long long nb, double* partials,
+                       unsigned int* counter, double* hist) {
     if (sc->done) return;
     __shared__ double red[32];
     const double alpha = sc->alpha, beta = sc->beta;
@@ -139,14 +146,16 @@ __global__ void k_zupd(const MinresScalars* sc, double* __restrict__ z, const do
     double o[1];
     block_sum<1>(acc, red, o);
     if (threadIdx.x == 0) partials[blockIdx.x] = o[0];
+    if (last_block(counter)) scalar_step(sc, partials, gridDim.x, hist, red);
 }
 
-__global__ void k_scalar(MinresScalars* sc, const double* __restrict__ partials, int nparts,
-                         double* hist) {
-    if (sc->done) return;
-    __shared__ double red[32];
+// The Givens step of one iteration from the |z|^2 partials, run by one whole
+// block (the last block of k_zupd): beta_new, the rotation, phi_bar, the
+// residual history and the stop test (MinresSolver.cpp:148-186).
+__device__ void scalar_step(MinresScalars* sc, const double* __restrict__ partials, int nparts,
+                            double* hist, double* red) {
     double acc[1] = {0.0};
-    for (int i = threadIdx.x; i < nparts; i += blockDim.x) acc[0] += partials[i];
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) acc[0] += __ldcg(partials + i);
     double o[1];
     block_sum<1>(acc, red, o);
     if (threadIdx.x != 0) return;
@@ -190,10 +199,10 @@ __global__ void k_scalar(MinresScalars* sc, const double* __restrict__ partials,
     }
 }
 
-__global__ void k_vwupd(const MinresScalars* sc, const double* __restrict__ z, const double* __restrict__ v,
+__global__ void k_vwupd(MinresScalars* sc, const double* __restrict__ z, const double* __restrict__ v,
                         double* __restrict__ v_new, double* __restrict__ w_prev_to_next,
                         const double* __restrict__ w, double* __restrict__ x, long long nb,
-                        double* partials) {
+                        double* partials, unsigned int* counter) {
     if (sc->done) return;
     __shared__ double red[4 * 32];
     const double beta_new = sc->beta_new, eps = sc->eps, delta = sc->delta, rho = sc->rho;
@@ -246,14 +255,17 @@ __global__ void k_vwupd(const MinresScalars* sc, const double* __restrict__ z, c
     block_sum<4>(acc, red, o);
     if (threadIdx.x == 0)
         for (int j = 0; j < 4; ++j) partials[4LL * blockIdx.x + j] = o[j];
+    if (last_block(counter)) finish_step(sc, partials, gridDim.x, red);
 }
 
-__global__ void k_finish(MinresScalars* sc, const double* __restrict__ partials, int nparts) {
-    if (sc->done) return;
-    __shared__ double red[4 * 32];
+// The end of one iteration, run by one whole block (the last block of
+// k_vwupd): component sums of v_new (the next apply's input mean), the
+// iteration counter, stop -> done.
+__device__ void finish_step(MinresScalars* sc, const double* __restrict__ partials, int nparts,
+                            double* red) {
     double acc[4] = {0, 0, 0, 0};
     for (int i = threadIdx.x; i < nparts; i += blockDim.x)
-        for (int j = 0; j < 4; ++j) acc[j] += partials[4LL * i + j];
+        for (int j = 0; j < 4; ++j) acc[j] += __ldcg(partials + 4LL * i + j);
     double o[4];
     block_sum<4>(acc, red, o);
     if (threadIdx.x == 0) {
@@ -261,6 +273,21 @@ __global__ void k_finish(MinresScalars* sc, const double* __restrict__ partials,
         sc->it += 1;
         if (sc->breakdown == 2) sc->done = 1;
     }
+}
+
+// true in every thread of the block that finishes last among the kernel's
+// blocks (its partial sums are then all in memory); the counter is reset
+__device__ __forceinline__ bool last_block(unsigned int* counter) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int t = atomicAdd(counter, 1u);
+        last = t == gridDim.x - 1;
+        if (last) *counter = 0u;
+    }
+    __syncthreads();
+    return last;
 }
 
 // ---- start-up kernels -------------------------------------------------------
@@ -515,11 +542,13 @@ cudaError_t minres_iteration(Problem& P) {
     const double inv_nb = 1.0 / (double)P.nb;
     FP_LAUNCHED(); k_alpha<<<1, 512, 0, P.stream>>>(P.d_sc, P.d_partials, nparts, inv_nb);
     const int blocks = vec_blocks(P, (P.nb + 1) / 2);
-    FP_LAUNCHED(); k_zupd<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, P.d_z, v, v_old, P.nb, P.d_partials);
-    FP_LAUNCHED(); k_scalar<<<1, 256, 0, P.stream>>>(P.d_sc, P.d_partials, blocks, P.d_hist);
+    // the last block of k_zupd runs the Givens step, the last block of
+    // k_vwupd the end of the iteration (block-count tickets in d_red)
+    unsigned int* tickets = reinterpret_cast<unsigned int*>(P.d_red + kTicketSlot);
+    FP_LAUNCHED(); k_zupd<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, P.d_z, v, v_old, P.nb, P.d_partials,
+                                                                tickets, P.d_hist);
     FP_LAUNCHED(); k_vwupd<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, P.d_z, v, v_new, w_prev, w, P.d_x, P.nb,
-                                                   P.d_partials);
-    FP_LAUNCHED(); k_finish<<<1, 256, 0, P.stream>>>(P.d_sc, P.d_partials, blocks);
+                                                                 P.d_partials, tickets + 1);
     return cudaGetLastError();
 }
 
