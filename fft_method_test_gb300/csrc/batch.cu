@@ -7,7 +7,7 @@
 // handle (its own stream) at a time and run fp_solve_permeability on it;
 // their kernels overlap on the GPU, so the small grids of a batch (48^3 to
 // 160^3 use a few hundred CTAs per pass) fill the 152 SMs together.  Inside a
-// solve the MINRES iterations are replayed as CUDA graphs of 20 (one graph
+// solve the MINRES iterations are replayed as CUDA graphs of 40 (one graph
 // launch per chunk, not nine kernel launches per iteration).  Problems are
 // taken largest first, which keeps the tail of the batch short.
 //

@@ -81,7 +81,9 @@ struct Problem {
     cudaStream_t stream = nullptr;
     int sm_count = 0;
     int tile_yz = 0;  // kx columns per CTA of the y and z passes (0 = default)
-    int reliable_interval = 20;  // mixed precision: true-residual check every this many iterations
+    // mixed precision: true-residual check every this many iterations (40:
+    // measured 2 % faster than 20 at 256^3 with the same iteration counts)
+    int reliable_interval = 40;
     // mixed precision: a refinement segment ends when the recurrence estimate
     // falls below this fraction of the segment's true residual
     double ahead_factor = 0.85;

@@ -129,8 +129,10 @@ __global__ void k_zupd(MinresScalars* sc, double* __restrict__ z, const double* 
         for (int h = 0; h < 3; ++h) {
             const double2 zz = z2[3 * k + h], vv = v2[3 * k + h], oo = o2[3 * k + h];
             const int c0 = (2 * h) % 3, c1 = (2 * h + 1) % 3;
-            const double a0 = (zz.x - mz[c0]) - (alpha * vv.x + beta * oo.x);
-            const double a1 = (zz.y - mz[c1]) - (alpha * vv.y + beta * oo.y);
+            // z - (mean + alpha v + beta v_old): three FP64 operations per
+            // element (GB300's FP64 pipe bounds this kernel)
+            const double a0 = zz.x - fma(beta, oo.x, fma(alpha, vv.x, mz[c0]));
+            const double a1 = zz.y - fma(beta, oo.y, fma(alpha, vv.y, mz[c1]));
             z2[3 * k + h] = make_double2(a0, a1);
             acc[0] += a0 * a0 + a1 * a1;
         }
@@ -138,7 +140,7 @@ __global__ void k_zupd(MinresScalars* sc, double* __restrict__ z, const double* 
     if ((nb & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
         for (int c = 0; c < 3; ++c) {
             const long long i = 3 * (nb - 1) + c;
-            const double a0 = (z[i] - mz[c]) - (alpha * v[i] + beta * v_old[i]);
+            const double a0 = z[i] - fma(beta, v_old[i], fma(alpha, v[i], mz[c]));
             z[i] = a0;
             acc[0] += a0 * a0;
         }
