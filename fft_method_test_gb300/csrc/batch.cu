@@ -8,7 +8,7 @@
 // their kernels overlap on the GPU, so the small grids of a batch (48^3 to
 // 160^3 use a few hundred CTAs per pass) fill the 152 SMs together.  Inside a
 // solve the MINRES iterations are replayed as CUDA graphs of 40 (one graph
-// launch per chunk, not nine kernel launches per iteration).  Problems are
+// launch per chunk, not eight kernel launches per iteration).  Problems are
 // taken largest first, which keeps the tail of the batch short.
 //
 // Autotuner.  The y and z passes take `tile` kx columns per CTA and have a
