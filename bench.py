@@ -478,6 +478,9 @@ def run_ours(args, world, rank, local):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         its_cpu = fx["iterations"] if fx else (it64b or its)
+        its_from = ("the CPU oracle's own iteration counts at tol %.0e" % fx["tol"] if fx else
+                    "the GPU %s solve's iteration counts (oracle fixture absent)"
+                    % ("FP64" if it64b else "mixed"))
         u = cpu_units(mask)
         cores = os.cpu_count() or 1
         cpu = {"value": cpu_predict(u, its_cpu, setups=3), "unit": UNIT, "cores": cores,
@@ -486,9 +489,8 @@ def run_ours(args, world, rank, local):
                          "(support + Green) %.2f s, one apply %.3f s and one MINRES iteration "
                          "(apply + vector work) %.3f s timed on this cell; seconds to K = 3 set-ups "
                          "(the reference recomputes Green per load case) + per load case 2 applies "
-                         "+ iterations x iteration time, with the CPU oracle's own iteration counts "
-                         "at tol %.0e (%s)" % (cores, u["setup_s"], u["apply_s"], u["iter_s"],
-                                               TOL_MIXED, its_cpu)}
+                         "+ iterations x iteration time, with %s (%s)"
+                         % (cores, u["setup_s"], u["apply_s"], u["iter_s"], its_from, its_cpu)}
 
     prob.close()
     if rank != 0:

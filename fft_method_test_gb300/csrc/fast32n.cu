@@ -1,0 +1,12 @@
+// fast32n.cu -- the specialised apply passes in FP32 for the edges with a
+// factor 3 or 5: 48, 80, 96, 160 (fft_fast.cuh).
+#include "fast_runners.cuh"
+
+namespace fp {
+namespace fast {
+template struct Passes<float, 48>;
+template struct Passes<float, 80>;
+template struct Passes<float, 96>;
+template struct Passes<float, 160>;
+}  // namespace fast
+}  // namespace fp

@@ -7,6 +7,76 @@
 #include "fft_fast.cuh"
 
 namespace fp {
+namespace fast {
+
+// per-edge dispatch to the runners of fast_runners.cuh (instantiated in
+// fast32.cu, fast64.cu, fast32n.cu, fast64n.cu)
+#define FP_EDGE_SWITCH(n, CALL)                    \
+    switch (n) {                                   \
+        case 32: return CALL(32);                  \
+        case 48: return CALL(48);                  \
+        case 64: return CALL(64);                  \
+        case 80: return CALL(80);                  \
+        case 96: return CALL(96);                  \
+        case 128: return CALL(128);                \
+        case 160: return CALL(160);                \
+        case 256: return CALL(256);                \
+        default: break;                            \
+    }
+
+template <typename T>
+cudaError_t run_xfwd(int n, const FastArgs& a, int grid, int threads, size_t smem, cudaStream_t s) {
+#define FP_CALL(N) Passes<T, N>::xfwd(a, grid, threads, smem, s)
+    FP_EDGE_SWITCH(n, FP_CALL)
+#undef FP_CALL
+    return cudaErrorInvalidValue;
+}
+
+template <typename T>
+cudaError_t run_xinv(int n, const FastArgs& a, int stage_bytes, int grid, int threads, size_t smem,
+                     cudaStream_t s) {
+#define FP_CALL(N) Passes<T, N>::xinv(a, stage_bytes, grid, threads, smem, s)
+    FP_EDGE_SWITCH(n, FP_CALL)
+#undef FP_CALL
+    return cudaErrorInvalidValue;
+}
+
+template <typename T>
+cudaError_t run_y(int n, int dir, const FastArgs& a, dim3 grid, cudaStream_t s) {
+#define FP_CALL(N) Passes<T, N>::y(dir, a, grid, s)
+    FP_EDGE_SWITCH(n, FP_CALL)
+#undef FP_CALL
+    return cudaErrorInvalidValue;
+}
+
+template <typename T>
+cudaError_t run_z(int n, int stages, const CUtensorMap& spec_map, const CUtensorMap& green_map,
+                  const FastArgs& a, dim3 grid, size_t smem, cudaStream_t s) {
+#define FP_CALL(N) Passes<T, N>::z(stages, spec_map, green_map, a, grid, smem, s)
+    FP_EDGE_SWITCH(n, FP_CALL)
+#undef FP_CALL
+    return cudaErrorInvalidValue;
+}
+
+template <typename T>
+int z_blocks_per_sm(int n, int stages, size_t smem) {
+#define FP_CALL(N) Passes<T, N>::z_per_sm(stages, smem)
+    FP_EDGE_SWITCH(n, FP_CALL)
+#undef FP_CALL
+    return 1;
+}
+
+template <typename T>
+int x_blocks_per_sm(int n, bool inverse, int threads, size_t smem) {
+#define FP_CALL(N) Passes<T, N>::x_per_sm(inverse, threads, smem)
+    FP_EDGE_SWITCH(n, FP_CALL)
+#undef FP_CALL
+    return 1;
+}
+
+#undef FP_EDGE_SWITCH
+
+}  // namespace fast
 
 bool fast_apply_supported(const Problem& P, int precision, int src_kind, int dst_kind, int stage) {
     (void)precision;

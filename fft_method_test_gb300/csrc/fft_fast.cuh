@@ -1,22 +1,20 @@
 // fft_fast.cuh -- the five apply passes specialised at compile time for the
-// power-of-two grid edges 32, 64, 128 and 256, for compact-vector operator
-// applies (scatter in, gather out).  The generic engine of fft_passes.cuh serves every other edge,
-// source and destination.
+// cubic grid edges 32, 48, 64, 80, 96, 128, 160 and 256, for compact-vector
+// operator applies (scatter in, gather out).  The generic engine of
+// fft_passes.cuh serves every other edge, source and destination.
 //
-// Each line of length N = R1 * R2 is transformed by TPL = R2 threads with the
-// four-step decomposition, one vector component per thread:
+// Each line of length N = R1 * R2 is transformed by TPL threads (TPL divides
+// R1 and R2) with the four-step decomposition, one vector component per
+// thread:
 //
 //   x[R2*i + a]  (i < R1, a < R2)
-//   stage A  thread owning a: DFT-R1 over i, times W_N^(S a k)  -> Y[k][a]
-//   stage B  thread owning k: DFT-R2 over a                      -> X[k + R1*m]
+//   stage A  threads owning a: DFT-R1 over i, times W_N^(S a k) -> Y[k][a]
+//   stage B  threads owning k: DFT-R2 over a                     -> X[k + R1*m]
 //
-// The inverse runs the same two stages with the radices swapped (R2 first),
-// so its stage A starts from exactly the values stage B of the forward
-// transform leaves with each owner: the z pass multiplies by the Green tensor
-// between the two without another exchange.  Only the Y exchange between the
-// stages (and the natural-order exchange around the Green multiply) goes
-// through shared memory; every stage reads or writes HBM directly where its
-// owner pattern is the natural one.
+// The inverse runs the same two stages with the radices swapped (R2 first).
+// Only the Y exchange between the stages (and the natural-order exchange
+// around the Green multiply) goes through shared memory; every stage reads
+// or writes HBM directly where its owner pattern is the natural one.
 //
 // Passes (kernels below):
 //   k_fx_fwd   scatter of the compact vector (minus its mean) into real
@@ -48,38 +46,92 @@
 namespace fp {
 namespace fast {
 
-// N = R1 * R2 with R1 >= R2; TPL = R2 threads per line.
+// N = R1 * R2 with R1 >= R2; TPL threads per line (TPL divides R1 and R2:
+// R2 for the powers of two, 4 for the edges with a factor 3 or 5).
 template <int N>
 struct Split;
 template <>
 struct Split<32> {
-    static constexpr int R1 = 8, R2 = 4;
+    static constexpr int R1 = 8, R2 = 4, TPL = 4;
+};
+template <>
+struct Split<48> {
+    static constexpr int R1 = 12, R2 = 4, TPL = 4;
 };
 template <>
 struct Split<64> {
-    static constexpr int R1 = 8, R2 = 8;
+    static constexpr int R1 = 8, R2 = 8, TPL = 8;
+};
+template <>
+struct Split<80> {
+    static constexpr int R1 = 20, R2 = 4, TPL = 4;
+};
+template <>
+struct Split<96> {
+    static constexpr int R1 = 12, R2 = 8, TPL = 4;
 };
 template <>
 struct Split<128> {
-    static constexpr int R1 = 16, R2 = 8;
+    static constexpr int R1 = 16, R2 = 8, TPL = 8;
+};
+template <>
+struct Split<160> {
+    static constexpr int R1 = 20, R2 = 8, TPL = 4;
 };
 template <>
 struct Split<256> {
-    static constexpr int R1 = 16, R2 = 16;
+    static constexpr int R1 = 16, R2 = 16, TPL = 16;
 };
 
 // ---- small DFTs in natural order -------------------------------------------
 
+template <int P, int Q, int S, typename T2>
+__device__ __forceinline__ void dft_pfa(T2 (&v)[P * Q]);
+
 // Natural-order DFT of R values (S = -1 forward, +1 backward) with the
-// radix kernels of fft_engine.cuh (2, 3, 4, 5, 8, 16).
+// radix kernels of fft_engine.cuh (2, 3, 4, 5, 8, 16); 12 = 4 x 3 and
+// 20 = 4 x 5 by the prime-factor algorithm.
 template <int R, int S, typename T2>
 __device__ __forceinline__ void dft_nat(T2 (&v)[R]) {
-    T2 t[R];
+    if constexpr (R == 12) {
+        dft_pfa<4, 3, S>(v);
+    } else if constexpr (R == 20) {
+        dft_pfa<4, 5, S>(v);
+    } else {
+        T2 t[R];
 #pragma unroll
-    for (int i = 0; i < R; ++i) t[i] = v[i];
-    dft_r<R, S>(t);
+        for (int i = 0; i < R; ++i) t[i] = v[i];
+        dft_r<R, S>(t);
 #pragma unroll
-    for (int k = 0; k < R; ++k) v[k] = t[out_slot<R>(k)];
+        for (int k = 0; k < R; ++k) v[k] = t[out_slot<R>(k)];
+    }
+}
+
+// Prime-factor (Good-Thomas) DFT of R = P * Q values, P and Q coprime: input
+// n = (Q n1 + P n2) mod R goes to a[n1][n2], length-Q DFTs along n2, then
+// length-P DFTs along n1, and output k is a[k mod P][k mod Q].  No twiddles
+// (Chinese-remainder index maps).
+template <int P, int Q, int S, typename T2>
+__device__ __forceinline__ void dft_pfa(T2 (&v)[P * Q]) {
+    constexpr int R = P * Q;
+    T2 a[P][Q];
+#pragma unroll
+    for (int n1 = 0; n1 < P; ++n1)
+#pragma unroll
+        for (int n2 = 0; n2 < Q; ++n2) a[n1][n2] = v[(Q * n1 + P * n2) % R];
+#pragma unroll
+    for (int n1 = 0; n1 < P; ++n1) dft_nat<Q, S>(a[n1]);
+#pragma unroll
+    for (int n2 = 0; n2 < Q; ++n2) {
+        T2 c[P];
+#pragma unroll
+        for (int n1 = 0; n1 < P; ++n1) c[n1] = a[n1][n2];
+        dft_nat<P, S>(c);
+#pragma unroll
+        for (int n1 = 0; n1 < P; ++n1) a[n1][n2] = c[n1];
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) v[k] = a[k % P][k % Q];
 }
 
 // twiddle W_N^(S e) from the table tw[j] = exp(-2 pi i j / N), 0 <= e < N
@@ -116,7 +168,7 @@ __host__ __device__ constexpr int col_ld() {
 template <int N, typename T>
 __host__ __device__ constexpr int x_ld() {
     constexpr int G = sizeof(T) == 4 ? 16 : 8;
-    constexpr int tpl = Split<N>::R2;
+    constexpr int tpl = Split<N>::TPL;
     constexpr int base = ((line_span<N>() + G - 1) / G) * G;
     return tpl < G ? base + tpl : base;
 }
@@ -156,6 +208,7 @@ template <int RA, int RB, int S, int TPL, bool SYNC, typename T2, class Load,
           class Bar = CtaBarrier>
 __device__ __forceinline__ void stage_a(T2* line, int t, bool active, const T2* __restrict__ tw,
                                         Load& load, Bar bar = Bar{}) {
+    static_assert(RB % TPL == 0, "owners per thread");
     constexpr int J = RB / TPL;
     T2 v[J][RA];
 #pragma unroll
@@ -185,6 +238,7 @@ template <int RA, int RB, int S, int TPL, bool SYNC, typename T2, class Store,
           class Bar = CtaBarrier>
 __device__ __forceinline__ void stage_b(const T2* line, int t, bool active, Store& store,
                                         Bar bar = Bar{}) {
+    static_assert(RA % TPL == 0, "owners per thread");
     constexpr int J = RA / TPL;
     T2 u[J][RB];
 #pragma unroll
@@ -248,7 +302,7 @@ __device__ __forceinline__ const double2* tw_of<double>(const FastArgs& a, int a
 // lines of TPL threads, rounded up to whole warps
 template <int N>
 __host__ __device__ constexpr int x_threads(int rows) {
-    return ((3 * rows / 2 * Split<N>::R2 + 31) / 32) * 32;
+    return ((3 * rows / 2 * Split<N>::TPL + 31) / 32) * 32;
 }
 
 // ---- cp.async (global -> shared, completion by group) ---------------------------
@@ -283,7 +337,7 @@ template <typename T, int N>
 __global__ void __launch_bounds__(384) k_fx_fwd(FastArgs a) {
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
-    constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = R2;
+    constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = Split<N>::TPL;
     constexpr int LD = x_ld<N, T>();
     constexpr int NH = N / 2 + 1;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -386,7 +440,7 @@ template <typename T, int N>
 __global__ void __launch_bounds__(384) k_fx_inv(FastArgs a, int stage_bytes) {
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
-    constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = R2;
+    constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = Split<N>::TPL;
     constexpr int LD = x_ld<N, T>();
     constexpr int NH = N / 2 + 1;
     constexpr int SPC = 16 / sizeof(T2);  // elements per 16-byte copy
@@ -502,10 +556,10 @@ __global__ void __launch_bounds__(384) k_fx_inv(FastArgs a, int stage_bytes) {
 
 // One CTA: TX kx columns of one z plane for one component (blockIdx.z).
 template <typename T, int N, int S, int TX>
-__global__ void __launch_bounds__(TX * Split<N>::R2) k_fcol_y(FastArgs a) {
+__global__ void __launch_bounds__(TX * Split<N>::TPL) k_fcol_y(FastArgs a) {
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
-    constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = R2;
+    constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = Split<N>::TPL;
     constexpr int LD = col_ld<N, T, TX>();
     __shared__ __align__(16) T2 lines[TX * LD];
     const int c = threadIdx.x % TX;
@@ -565,12 +619,12 @@ __host__ __device__ constexpr size_t z_stage_bytes() {
 // barrier 1 + comp); the Green multiply reads all three.  Waits are bounded:
 // on a timeout the CTA raises a.err and returns.
 template <typename T, int N, int TX, int STAGES>
-__global__ void __launch_bounds__(3 * TX * Split<N>::R2, STAGES == 1 ? 3 : 1)
+__global__ void __launch_bounds__(3 * TX * Split<N>::TPL, STAGES == 1 ? 3 : 1)
     k_fz(const __grid_constant__ CUtensorMap spec_map, const __grid_constant__ CUtensorMap green_map,
          FastArgs a) {
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
-    constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = R2;
+    constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = Split<N>::TPL;
     constexpr int LD = col_ld<N, T, TX>();
     constexpr int CS = comp_stride<T, N, TX>();
     constexpr size_t STAGE = z_stage_bytes<T, N, TX>();
@@ -703,46 +757,68 @@ constexpr int z_tx() {
 }
 
 // grid edges with specialised kernels
-inline bool edge_supported(int n) { return n == 32 || n == 64 || n == 128 || n == 256; }
+#define FP_FAST_EDGES(CALL) CALL(32) CALL(48) CALL(64) CALL(80) CALL(96) CALL(128) CALL(160) CALL(256)
 
-// grid rows per tile of the x passes: about 192 threads per CTA
+inline bool edge_supported(int n) {
+#define FP_CASE(N) if (n == N) return true;
+    FP_FAST_EDGES(FP_CASE)
+#undef FP_CASE
+    return false;
+}
+
+// grid rows per tile of the x passes: about 192 threads per CTA, 96 where
+// the lines are long and served by 4 threads (shared memory)
 inline int x_rows_for(int n) {
     switch (n) {
         case 32: return 32;
+        case 48: return 32;
         case 64: return 16;
+        case 80: return 32;
+        case 96: return 16;
         case 128: return 16;
+        case 160: return 16;
         default: return 8;
     }
 }
 inline int x_tpl(int n) {
-    switch (n) {
-        case 32: return Split<32>::R2;
-        case 64: return Split<64>::R2;
-        case 128: return Split<128>::R2;
-        default: return Split<256>::R2;
-    }
+#define FP_CASE(N) if (n == N) return Split<N>::TPL;
+    FP_FAST_EDGES(FP_CASE)
+#undef FP_CASE
+    return 0;
 }
 template <typename T>
 int x_ld_rt(int n) {
-    switch (n) {
-        case 32: return x_ld<32, T>();
-        case 64: return x_ld<64, T>();
-        case 128: return x_ld<128, T>();
-        default: return x_ld<256, T>();
-    }
+#define FP_CASE(N) if (n == N) return x_ld<N, T>();
+    FP_FAST_EDGES(FP_CASE)
+#undef FP_CASE
+    return 0;
 }
 
 // dynamic shared memory of the z pass: mbarriers + its pipeline stages
 template <typename T>
 size_t z_smem_rt(int n, int stages) {
     constexpr int TX = z_tx<T>();
-    switch (n) {
-        case 32: return 128 + stages * z_stage_bytes<T, 32, TX>();
-        case 64: return 128 + stages * z_stage_bytes<T, 64, TX>();
-        case 128: return 128 + stages * z_stage_bytes<T, 128, TX>();
-        default: return 128 + stages * z_stage_bytes<T, 256, TX>();
-    }
+#define FP_CASE(N) if (n == N) return 128 + stages * z_stage_bytes<T, N, TX>();
+    FP_FAST_EDGES(FP_CASE)
+#undef FP_CASE
+    return 0;
 }
+
+// Launch runners of one edge, defined in fast_runners.cuh and instantiated
+// per precision and edge group (fast32.cu, fast64.cu: powers of two;
+// fast32n.cu, fast64n.cu: 48, 80, 96, 160) so that they build in parallel.
+template <typename T, int N>
+struct Passes {
+    static cudaError_t xfwd(const FastArgs& a, int grid, int threads, size_t smem, cudaStream_t s);
+    static cudaError_t xinv(const FastArgs& a, int stage_bytes, int grid, int threads, size_t smem,
+                            cudaStream_t s);
+    static cudaError_t y(int dir, const FastArgs& a, dim3 grid, cudaStream_t s);
+    static cudaError_t z(int stages, const CUtensorMap& spec_map, const CUtensorMap& green_map,
+                         const FastArgs& a, dim3 grid, size_t smem, cudaStream_t s);
+    // blocks resident per SM at this shared-memory size
+    static int z_per_sm(int stages, size_t smem);
+    static int x_per_sm(bool inverse, int threads, size_t smem);
+};
 
 template <typename T>
 cudaError_t run_xfwd(int n, const FastArgs& a, int grid, int threads, size_t smem, cudaStream_t s);

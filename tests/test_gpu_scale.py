@@ -8,8 +8,9 @@ golden fixtures directly.
   reference build).  Both solves stop at a relative MINRES residual of 1e-10;
   K agrees to 1e-9 relative (the solves' own residual level), and to 1e-6 for
   mixed precision at tol 1e-7.
-* Operator applies on the specialised power-of-two passes against the oracle
-  (1e-12 FP64, 5e-6 mixed) and against the generic passes (FFTPERM_NO_FAST).
+* Operator applies on the specialised passes (edges 32 to 256 with factors
+  2, 3, 5) against the oracle (1e-12 FP64, 5e-6 mixed) and against the
+  generic passes (FFTPERM_NO_FAST).
 * The reference-built fixtures of tests/golden/golden.npz (C1 K, the 16^3
   apply and RHS, the non-cubic Green table) read straight into GPU checks.
 """
@@ -69,10 +70,12 @@ def test_mixed_permeability_at_scale_within_1e6(gpu_lib, name):
 
 
 @pytest.mark.parametrize("shape", [(32, 32, 32), (64, 64, 64), (128, 128, 128), (64, 32, 128),
-                                   (256, 128, 64)])
+                                   (256, 128, 64), (48, 48, 48), (80, 80, 80), (96, 80, 160),
+                                   (160, 96, 48)])
 def test_specialised_apply_matches_oracle(gpu_lib, restatement, shape):
-    """Power-of-two edges run the specialised passes: FP64 apply to 1e-12 and
-    mixed to FP32 accuracy against the oracle."""
+    """Edges 32, 48, 64, 80, 96, 128, 160 and 256 run the specialised passes
+    (radix-12 and radix-20 four-step lines for the edges with a factor 3 or
+    5): FP64 apply to 1e-12 and mixed to FP32 accuracy against the oracle."""
     mask = G.gaussian_field(shape, 4.0, 0.4, seed=sum(shape))
     ctx = restatement.context(mask)
     x = np.random.default_rng(5).uniform(-1, 1, 3 * ctx.nb)
@@ -87,9 +90,9 @@ def test_specialised_apply_matches_oracle(gpu_lib, restatement, shape):
     assert rel_err(y32, y_ref) < 5e-6
 
 
+@pytest.mark.parametrize("shape", [(64, 128, 64), (160, 48, 96)])
 @pytest.mark.parametrize("precision,bar", [("fp64", 1e-13), ("mixed", 2e-6)])
-def test_specialised_passes_match_generic(gpu_lib, precision, bar):
-    shape = (64, 128, 64)
+def test_specialised_passes_match_generic(gpu_lib, precision, bar, shape):
     mask = G.gaussian_field(shape, 5.0, 0.35, seed=9)
     x = None
     out = []
