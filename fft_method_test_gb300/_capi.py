@@ -37,7 +37,8 @@ EXPORTED = [
     "fp_solve_load_case", "fp_solve_permeability", "fp_brinkman_solve",
     "fp_brinkman_permeability", "fp_brinkman_last_error", "fp_green_apply_noalloc",
     "fp_kernel_launch_count", "fp_brinkman_fft_solve", "fp_brinkman_fft_permeability",
-    "fp_autotune", "fp_set_tiling", "fp_batch_solve_permeability", "fp_batch_last_error", "fp_write_fvel",
+    "fp_autotune", "fp_set_tiling", "fp_batch_solve_permeability", "fp_batch_solve_grouped",
+    "fp_group_solve_permeability", "fp_batch_last_error", "fp_write_fvel",
     "fp_nn_conv", "fp_nn_wgrad", "fp_nn_bias_grad", "fp_nn_relu_back", "fp_nn_adam", "fp_nn_loss",
     "fp_measure_fp64_rate", "fp_nn_conv_tc", "fp_nn_tc_error", "fp_nn_pool2", "fp_nn_pool2_back",
     "fp_nn_up2_add", "fp_nn_up2_add_back", "fp_nn_wgrad_cc", "fp_time_apply",
@@ -124,6 +125,11 @@ _SIGNATURES = {
     "fp_batch_solve_permeability": ([C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
                                      C.c_int, C.c_int, C.c_int, C.c_double, C.c_int64, C.c_int,
                                      C.c_int, _dp, C.c_void_p, C.c_void_p], C.c_int),
+    "fp_batch_solve_grouped": ([C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                C.c_int, C.c_int, C.c_int, C.c_double, C.c_int64, C.c_int,
+                                C.c_int, C.c_int, _dp, C.c_void_p, C.c_void_p], C.c_int),
+    "fp_group_solve_permeability": ([C.c_int, C.c_void_p, C.c_double, C.c_int64, _dp, C.c_void_p],
+                                     C.c_int),
     "fp_batch_last_error": ([], C.c_char_p),
     "fp_nn_conv": ([C.c_int, C.c_int, C.c_int, C.c_int64, C.c_int, C.c_int, C.c_void_p, C.c_int,
                     C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p],

@@ -3,13 +3,15 @@
 //
 // Batching.  Each microstructure is a complete permeability solve (three load
 // cases) with no data shared with the others, so the batch needs no
-// collective: it is a work queue.  `concurrency` host threads each own one
-// handle (its own stream) at a time and run fp_solve_permeability on it;
-// their kernels overlap on the GPU, so the small grids of a batch (48^3 to
-// 160^3 use a few hundred CTAs per pass) fill the 152 SMs together.  Inside a
-// solve the MINRES iterations are replayed as CUDA graphs of 40 (one graph
-// launch per chunk, not eight kernel launches per iteration).  Problems are
-// taken largest first, which keeps the tail of the batch short.
+// collective: it is a work queue.  The problems are cut into groups of up to
+// `max_group` problems of one grid and voxel size; `concurrency` host threads
+// each take one group at a time (its own stream) and solve it with
+// fp_group_solve_permeability (one lockstep MINRES per load case over the
+// group, one launch per pass for all members) or, for a group of one, with
+// fp_solve_permeability, whose MINRES iterations are replayed as CUDA graphs
+// of 40.  The threads' kernels overlap on the GPU, so the small grids of a
+// batch fill the 152 SMs together.  Groups are taken largest first, which
+// keeps the tail of the batch short.
 //
 // Autotuner.  The y and z passes take `tile` kx columns per CTA and have a
 // TMA-fed and a register-fed variant; the inverse x pass has a bulk-copy
@@ -177,11 +179,6 @@ int tune(Problem& P, TuneResult* out) {
     return FP_OK;
 }
 
-struct Job {
-    int index;
-    long long voxels;
-};
-
 }  // namespace
 }  // namespace fp
 
@@ -229,9 +226,18 @@ extern "C" int fp_batch_solve_permeability(int count, const int* dims, const uin
                                            int precision, int support_mode, double tol,
                                            int64_t maxit, int concurrency, int autotune, double* K,
                                            fp_solver_stats* stats, int* status) {
+    return fp_batch_solve_grouped(count, dims, masks, voxel_sizes, mu, p_radius, precision, support_mode,
+                                  tol, maxit, concurrency, autotune, 1, K, stats, status);
+}
+
+extern "C" int fp_batch_solve_grouped(int count, const int* dims, const uint8_t* const* masks,
+                                      const double* voxel_sizes, double mu, int p_radius,
+                                      int precision, int support_mode, double tol, int64_t maxit,
+                                      int concurrency, int autotune, int max_group, double* K,
+                                      fp_solver_stats* stats, int* status) {
     using namespace fp;
     g_batch_error.clear();
-    if (count < 0 || (count > 0 && (!dims || !masks || !K)) || concurrency < 1) {
+    if (count < 0 || (count > 0 && (!dims || !masks || !K)) || concurrency < 1 || max_group < 1) {
         g_batch_error = "batch: invalid arguments";
         return FP_ERR_INVALID;
     }
@@ -271,11 +277,26 @@ extern "C" int fp_batch_solve_permeability(int count, const int* dims, const uin
             fp_destroy(h);
         }
     }
-    // 2) largest first
-    std::vector<Job> jobs((size_t)count);
+    // 2) jobs: groups of up to max_group problems of one grid and voxel size
+    //    (one lockstep solve each), largest total first
+    std::map<std::tuple<int, int, int, double>, std::vector<int>> by_grid;
     for (int i = 0; i < count; ++i)
-        jobs[(size_t)i] = Job{i, (long long)dims[3 * i] * dims[3 * i + 1] * dims[3 * i + 2]};
-    std::stable_sort(jobs.begin(), jobs.end(), [](const Job& a, const Job& b) { return a.voxels > b.voxels; });
+        by_grid[std::make_tuple(dims[3 * i], dims[3 * i + 1], dims[3 * i + 2],
+                                voxel_sizes ? voxel_sizes[i] : 1.0)]
+            .push_back(i);
+    std::vector<std::vector<int>> groups;
+    for (auto& kv : by_grid)
+        for (size_t k = 0; k < kv.second.size(); k += (size_t)max_group)
+            groups.emplace_back(kv.second.begin() + k,
+                                kv.second.begin() + std::min(kv.second.size(), k + (size_t)max_group));
+    auto voxels = [&](const std::vector<int>& g) {
+        long long v = 0;
+        for (int i : g) v += (long long)dims[3 * i] * dims[3 * i + 1] * dims[3 * i + 2];
+        return v;
+    };
+    std::stable_sort(groups.begin(), groups.end(),
+                     [&](const std::vector<int>& a, const std::vector<int>& b) { return voxels(a) > voxels(b); });
+    const int njobs = (int)groups.size();
     std::atomic<int> next{0};
     std::vector<int> rcs((size_t)count, FP_OK);
     std::vector<std::string> errs((size_t)count);
@@ -283,24 +304,48 @@ extern "C" int fp_batch_solve_permeability(int count, const int* dims, const uin
         cudaSetDevice(dev);
         for (;;) {
             const int j = next.fetch_add(1);
-            if (j >= count) return;
-            const int i = jobs[(size_t)j].index;
-            fp_handle h = nullptr;
-            int rc = make(i, &h);
-            if (rc == FP_OK && autotune) {
-                TuneResult r;
-                rc = tune(h->P, &r);  // a cache hit: sets the tuned tiling
+            if (j >= njobs) return;
+            const std::vector<int>& g = groups[(size_t)j];
+            const int G = (int)g.size();
+            std::vector<fp_handle> hs((size_t)G, nullptr);
+            int rc = FP_OK;
+            int bad = g[0];
+            for (int k = 0; k < G && rc == FP_OK; ++k) {
+                bad = g[(size_t)k];
+                rc = make(bad, &hs[(size_t)k]);
+                if (rc == FP_OK && autotune) {
+                    TuneResult r;
+                    rc = tune(hs[(size_t)k]->P, &r);  // a cache hit: sets the tuned tiling
+                }
             }
-            fp_solver_stats st[3] = {};
-            if (rc == FP_OK) rc = fp_solve_permeability(h, tol, maxit, K + 9 * (size_t)i, st);
-            if (rc == FP_OK && stats)
-                for (int c = 0; c < 3; ++c) stats[3 * (size_t)i + c] = st[c];
-            if (rc != FP_OK) errs[(size_t)i] = h ? h->P.err : std::string("create failed");
-            rcs[(size_t)i] = rc;
-            fp_destroy(h);
+            std::vector<double> Kg((size_t)9 * G);
+            std::vector<fp_solver_stats> st((size_t)3 * G);
+            if (rc == FP_OK) {
+                rc = G == 1 ? fp_solve_permeability(hs[0], tol, maxit, Kg.data(), st.data())
+                            : fp_group_solve_permeability(G, hs.data(), tol, maxit, Kg.data(), st.data());
+                if (rc != FP_OK) {
+                    bad = g[0];
+                    for (int k = 0; k < G; ++k)
+                        if (!hs[(size_t)k]->P.err.empty()) bad = g[(size_t)k];
+                }
+            }
+            for (int k = 0; k < G; ++k) {
+                const int i = g[(size_t)k];
+                if (rc == FP_OK) {
+                    for (int q = 0; q < 9; ++q) K[9 * (size_t)i + q] = Kg[9 * (size_t)k + q];
+                    if (stats)
+                        for (int c = 0; c < 3; ++c) stats[3 * (size_t)i + c] = st[3 * (size_t)k + c];
+                } else {
+                    const int kb = (int)(std::find(g.begin(), g.end(), bad) - g.begin());
+                    errs[(size_t)i] = (kb < G && hs[(size_t)kb]) ? hs[(size_t)kb]->P.err
+                                                                 : std::string("create failed");
+                }
+                rcs[(size_t)i] = rc;
+            }
+            for (fp_handle h : hs) fp_destroy(h);
         }
     };
-    const int nthreads = std::min(concurrency, std::max(count, 1));
+    const int nthreads = std::min(concurrency, std::max(njobs, 1));
     std::vector<std::thread> pool;
     for (int t = 0; t < nthreads; ++t) pool.emplace_back(worker);
     for (auto& t : pool) t.join();

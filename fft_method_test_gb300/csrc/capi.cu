@@ -273,8 +273,25 @@ int read_scalars(Problem& P) {
 // P.ahead_factor = 0.85 of it).  The FP64 residual |b - A x| then decides:
 // below tol the solve has converged, otherwise a new segment starts from x.  The reported
 // residual is that FP64 residual; the history holds the last segment.
-int device_minres(Problem& P, const double* d_b, const double* d_x0, double tol, long long maxit,
-                  double* hist_host, fp_solver_stats* st) {
+// State of one MINRES solve between chunks of iterations: device_minres runs
+// one, group_minres runs several problems of one grid in lockstep.
+struct MinresRun {
+    Problem* P = nullptr;
+    const double* d_b = nullptr;
+    double tol = 0.0;
+    long long maxit = 0;
+    bool mixed = false;
+    int chunk = 16;
+    const double* seg_x0 = nullptr;  // null: the segment starts from zero
+    long long done_its = 0;          // iterations of finished segments
+    int restarts = 0;
+    double rel64 = -1.0;
+    bool converged64 = false;
+    bool finished = false;
+};
+
+int minres_begin(MinresRun& r, Problem& P, const double* d_b, const double* d_x0, double tol,
+                 long long maxit) {
     if (!(tol > 0.0)) return fail(P, FP_ERR_INVALID, "MinresSolver tolerance must be positive");
     if (maxit + 1 > P.hist_cap) {
         fp::release_graphs(P);  // the graphs write the history through the old pointer
@@ -283,76 +300,81 @@ int device_minres(Problem& P, const double* d_b, const double* d_x0, double tol,
         FP_CUDA(dalloc(P, &P.d_hist, (size_t)maxit + 1), "cudaMalloc hist");
         P.hist_cap = maxit + 1;
     }
-    const bool mixed = P.precision == fp::kMixed && P.reliable_interval > 0;
-    if (mixed) {
+    r = MinresRun{};
+    r.P = &P;
+    r.d_b = d_b;
+    r.tol = tol;
+    r.maxit = maxit;
+    r.mixed = P.precision == fp::kMixed && P.reliable_interval > 0;
+    if (r.mixed) {
         int rc = ensure_green_both(P);
         if (rc) return rc;
     }
     const size_t bytes = sizeof(double) * 3 * (size_t)P.nb;
     // the first segment's r0 uses the FP64 operator in mixed mode
-    FP_CUDA(fp::minres_start(P, d_b, d_x0, tol, maxit, mixed ? fp::kFP64 : -1), "minres_start");
-    const double* seg_x0 = d_x0;  // null: the segment starts from zero
-    if (mixed) {
+    FP_CUDA(fp::minres_start(P, d_b, d_x0, tol, maxit, r.mixed ? fp::kFP64 : -1), "minres_start");
+    r.seg_x0 = d_x0;
+    if (r.mixed) {
         FP_CUDA(cudaMemcpyAsync(P.d_r0, P.d_z, bytes, cudaMemcpyDeviceToDevice, P.stream), "copy");
         if (d_x0) {
             FP_CUDA(cudaMemcpyAsync(P.d_corr, d_x0, bytes, cudaMemcpyDeviceToDevice, P.stream),
                     "copy");
-            seg_x0 = P.d_corr;  // keep the start point (d_x0 may alias P.d_cin)
+            r.seg_x0 = P.d_corr;  // keep the start point (d_x0 may alias P.d_cin)
         }
     }
-    {
-        int rc = read_scalars(P);
+    r.chunk = r.mixed ? P.reliable_interval : 16;
+    return read_scalars(P);
+}
+
+// After a chunk of iterations (or none, once the recurrence is done): the
+// mixed-mode segment test, FP64 residual and restart; sets r.finished.
+int minres_step(MinresRun& r) {
+    Problem& P = *r.P;
+    constexpr int max_restarts = 20;
+    if (!r.mixed) {
+        if (P.h_sc->done) r.finished = true;
+        return FP_OK;
+    }
+    const size_t bytes = sizeof(double) * 3 * (size_t)P.nb;
+    const fp::MinresScalars s = *P.h_sc;
+    const long long total = r.done_its + s.it;
+    // the segment's true residual |r0 - A32 (x - x0)| / |b|
+    double seg_rel = 0.0;
+    if (!s.done || !s.converged) {
+        const double* y = P.d_x;
+        if (r.seg_x0) {
+            FP_CUDA(fp::launch_axpby(P, P.d_cin, 1.0, P.d_x, -1.0, r.seg_x0), "diff");
+            y = P.d_cin;
+        }
+        int rc = residual_norm(P, P.d_r0, y, fp::kMixed, s.rhs_norm, &seg_rel);
         if (rc) return rc;
     }
-    const int chunk = mixed ? P.reliable_interval : 16;
-    long long done_its = 0;  // iterations of finished segments
-    int restarts = 0;
-    double rel64 = -1.0;
-    bool converged64 = false;
-    const int max_restarts = 20;
-    for (;;) {
-        if (!P.h_sc->done) {
-            FP_CUDA(fp::minres_iterations(P, chunk), "minres_iteration");
-            int rc = read_scalars(P);
-            if (rc) return rc;
-        }
-        if (!mixed) {
-            if (P.h_sc->done) break;
-            continue;
-        }
-        const fp::MinresScalars s = *P.h_sc;
-        const long long total = done_its + s.it;
-        // the segment's true residual |r0 - A32 (x - x0)| / |b|
-        double seg_rel = 0.0;
-        if (!s.done || !s.converged) {
-            const double* y = P.d_x;
-            if (seg_x0) {
-                FP_CUDA(fp::launch_axpby(P, P.d_cin, 1.0, P.d_x, -1.0, seg_x0), "diff");
-                y = P.d_cin;
-            }
-            int rc = residual_norm(P, P.d_r0, y, fp::kMixed, s.rhs_norm, &seg_rel);
-            if (rc) return rc;
-        }
-        const bool seg_end =
-            s.done || seg_rel <= P.segment_tol_factor * tol || s.rel_res < P.ahead_factor * seg_rel;
-        if (!seg_end) continue;
-        int rc = residual_norm(P, d_b, P.d_x, fp::kFP64, s.rhs_norm, &rel64);
-        if (rc) return rc;
-        if (rel64 <= tol) {
-            converged64 = true;
-            break;
-        }
-        if (total >= maxit || restarts >= max_restarts) break;
-        // next segment from the current iterate, r0 with the FP64 operator
-        FP_CUDA(cudaMemcpyAsync(P.d_corr, P.d_x, bytes, cudaMemcpyDeviceToDevice, P.stream), "copy");
-        seg_x0 = P.d_corr;
-        done_its = total;
-        ++restarts;
-        FP_CUDA(fp::minres_start(P, d_b, P.d_corr, tol, maxit - total, fp::kFP64), "minres_start");
-        FP_CUDA(cudaMemcpyAsync(P.d_r0, P.d_z, bytes, cudaMemcpyDeviceToDevice, P.stream), "copy");
-        rc = read_scalars(P);
-        if (rc) return rc;
+    const bool seg_end =
+        s.done || seg_rel <= P.segment_tol_factor * r.tol || s.rel_res < P.ahead_factor * seg_rel;
+    if (!seg_end) return FP_OK;
+    int rc = residual_norm(P, r.d_b, P.d_x, fp::kFP64, s.rhs_norm, &r.rel64);
+    if (rc) return rc;
+    if (r.rel64 <= r.tol) {
+        r.converged64 = true;
+        r.finished = true;
+        return FP_OK;
     }
+    if (total >= r.maxit || r.restarts >= max_restarts) {
+        r.finished = true;
+        return FP_OK;
+    }
+    // next segment from the current iterate, r0 with the FP64 operator
+    FP_CUDA(cudaMemcpyAsync(P.d_corr, P.d_x, bytes, cudaMemcpyDeviceToDevice, P.stream), "copy");
+    r.seg_x0 = P.d_corr;
+    r.done_its = total;
+    ++r.restarts;
+    FP_CUDA(fp::minres_start(P, r.d_b, P.d_corr, r.tol, r.maxit - total, fp::kFP64), "minres_start");
+    FP_CUDA(cudaMemcpyAsync(P.d_r0, P.d_z, bytes, cudaMemcpyDeviceToDevice, P.stream), "copy");
+    return read_scalars(P);
+}
+
+int minres_finish(MinresRun& r, double* hist_host, fp_solver_stats* st) {
+    Problem& P = *r.P;
     const fp::MinresScalars s = *P.h_sc;
     {
         const int erc = check_device_error(P);
@@ -365,17 +387,69 @@ int device_minres(Problem& P, const double* d_b, const double* d_x0, double tol,
         FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
     }
     if (st) {
-        st->iterations = done_its + s.it;
-        if (mixed) {
-            st->final_rel_residual = rel64;
-            st->converged = converged64 ? 1 : 0;
+        st->iterations = r.done_its + s.it;
+        if (r.mixed) {
+            st->final_rel_residual = r.rel64;
+            st->converged = r.converged64 ? 1 : 0;
         } else {
             st->final_rel_residual = s.rel_res;
-            st->converged = s.converged ? 1 : (s.rel_res <= tol ? 1 : 0);
+            st->converged = s.converged ? 1 : (s.rel_res <= r.tol ? 1 : 0);
         }
-        st->refinements = restarts;
+        st->refinements = r.restarts;
     }
     return FP_OK;
+}
+
+int device_minres(Problem& P, const double* d_b, const double* d_x0, double tol, long long maxit,
+                  double* hist_host, fp_solver_stats* st) {
+    MinresRun r;
+    int rc = minres_begin(r, P, d_b, d_x0, tol, maxit);
+    if (rc) return rc;
+    while (!r.finished) {
+        if (!P.h_sc->done) {
+            FP_CUDA(fp::minres_iterations(P, r.chunk), "minres_iteration");
+            rc = read_scalars(P);
+            if (rc) return rc;
+        }
+        rc = minres_step(r);
+        if (rc) return rc;
+    }
+    return minres_finish(r, hist_host, st);
+}
+
+// Lockstep MINRES of the problems of runs (one grid, one stream): while two
+// or more still iterate, each chunk runs through group_iterations (one launch
+// per pass for all of them); a lone member takes the single path.  After each
+// chunk every unfinished member runs its own segment logic.
+int group_minres(std::vector<MinresRun>& runs, fp::GroupTables* tab) {
+    for (;;) {
+        std::vector<Problem*> act;
+        bool any = false;
+        int chunk = 0;
+        for (auto& r : runs) {
+            if (r.finished) continue;
+            any = true;
+            chunk = r.chunk;
+            if (!r.P->h_sc->done) act.push_back(r.P);
+        }
+        if (!any) return FP_OK;
+        if (act.size() == 1) {
+            Problem& P = *act[0];
+            FP_CUDA(fp::minres_iterations(P, chunk), "minres_iteration");
+        } else if (act.size() > 1) {
+            Problem& P = *act[0];
+            FP_CUDA(fp::group_iterations(act.data(), (int)act.size(), chunk, tab), "group iteration");
+        }
+        for (Problem* m : act) {
+            int rc = read_scalars(*m);
+            if (rc) return rc;
+        }
+        for (auto& r : runs) {
+            if (r.finished) continue;
+            int rc = minres_step(r);
+            if (rc) return rc;
+        }
+    }
 }
 
 // v = G*(f0 + P_B x) - mean_B(...), avg = <v> over the domain
@@ -927,6 +1001,80 @@ int fp_solve_permeability(fp_handle h, double tol, int64_t maxit, double K[9],
         if (stats) stats[col] = st;
     }
     return FP_OK;
+}
+
+int fp_group_solve_permeability(int count, fp_handle* handles, double tol, int64_t maxit, double* K,
+                                fp_solver_stats* stats) {
+    if (count < 1 || !handles || !K) return FP_ERR_INVALID;
+    for (int i = 0; i < count; ++i)
+        if (!handles[i]) return FP_ERR_INVALID;
+    Problem& P0 = handles[0]->P;
+    for (int i = 0; i < count; ++i) {
+        Problem& P = handles[i]->P;
+        int rc = need_geometry(P, "PermeabilityRunner::run");
+        if (rc) return rc;
+        if (P.nx != P0.nx || P.ny != P0.ny || P.nz != P0.nz || P.precision != P0.precision ||
+            P.reliable_interval != P0.reliable_interval)
+            return fail(P, FP_ERR_INVALID, "group: members must share grid, precision and reliable interval");
+    }
+    bool grouped = count > 1;
+    for (int i = 0; i < count && grouped; ++i) grouped = fp::group_supported(handles[i]->P);
+    if (!grouped) {  // one at a time on the members' own streams
+        for (int i = 0; i < count; ++i) {
+            int rc = fp_solve_permeability(handles[i], tol, maxit, K + 9 * (size_t)i,
+                                           stats ? stats + 3 * (size_t)i : nullptr);
+            if (rc) return rc;
+        }
+        return FP_OK;
+    }
+    // every member on the first member's stream for the duration
+    std::vector<cudaStream_t> own((size_t)count);
+    for (int i = 0; i < count; ++i) {
+        Problem& P = handles[i]->P;
+        own[(size_t)i] = P.stream;
+        FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+        P.stream = P0.stream;
+    }
+    fp::GroupTables* tab = nullptr;
+    auto restore = [&](int rc) {
+        cudaStreamSynchronize(P0.stream);
+        for (int i = 0; i < count; ++i) handles[i]->P.stream = own[(size_t)i];
+        fp::group_tables_destroy(tab);
+        return rc;
+    };
+    const int chunk = P0.precision == fp::kMixed && P0.reliable_interval > 0 ? P0.reliable_interval : 16;
+    {
+        cudaError_t e = fp::group_tables_create(&tab, count, chunk);
+        if (e != cudaSuccess) return restore(cuda_fail(P0, e, "group tables"));
+    }
+    std::vector<MinresRun> runs((size_t)count);
+    for (int col = 0; col < 3; ++col) {
+        double g[3] = {0.0, 0.0, 0.0};
+        g[col] = 1.0;
+        const double t0 = now_s();
+        for (int i = 0; i < count; ++i) {
+            Problem& P = handles[i]->P;
+            int rc = device_build_rhs(P, g, P.d_b);
+            if (!rc) rc = minres_begin(runs[(size_t)i], P, P.d_b, nullptr, tol, maxit);
+            if (rc) return restore(rc);
+        }
+        int rc = group_minres(runs, tab);
+        if (rc) return restore(rc);
+        for (int i = 0; i < count; ++i) {
+            Problem& P = handles[i]->P;
+            fp_solver_stats st{};
+            rc = minres_finish(runs[(size_t)i], nullptr, &st);
+            double avg[3];
+            if (!rc) rc = device_recover(P, g, P.d_x, avg, false);
+            if (rc) return restore(rc);
+            // colK = -mu <v>; set_column stores -colK (PermeabilityRunner.cpp:772-777,
+            // PermeabilityTensor.cpp:16)
+            for (int row = 0; row < 3; ++row) K[9 * (size_t)i + row * 3 + col] = -(-P.mu * avg[row]);
+            st.seconds = now_s() - t0;
+            if (stats) stats[3 * (size_t)i + col] = st;
+        }
+    }
+    return restore(FP_OK);
 }
 
 }  // extern "C"

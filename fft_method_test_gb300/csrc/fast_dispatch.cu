@@ -25,7 +25,7 @@ namespace fast {
     }
 
 template <typename T>
-cudaError_t run_xfwd(int n, const FastArgs& a, int grid, int threads, size_t smem, cudaStream_t s) {
+cudaError_t run_xfwd(int n, const FastArgs& a, dim3 grid, int threads, size_t smem, cudaStream_t s) {
 #define FP_CALL(N) Passes<T, N>::xfwd(a, grid, threads, smem, s)
     FP_EDGE_SWITCH(n, FP_CALL)
 #undef FP_CALL
@@ -33,7 +33,7 @@ cudaError_t run_xfwd(int n, const FastArgs& a, int grid, int threads, size_t sme
 }
 
 template <typename T>
-cudaError_t run_xinv(int n, const FastArgs& a, int stage_bytes, int grid, int threads, size_t smem,
+cudaError_t run_xinv(int n, const FastArgs& a, int stage_bytes, dim3 grid, int threads, size_t smem,
                      cudaStream_t s) {
 #define FP_CALL(N) Passes<T, N>::xinv(a, stage_bytes, grid, threads, smem, s)
     FP_EDGE_SWITCH(n, FP_CALL)
@@ -85,10 +85,24 @@ bool fast_apply_supported(const Problem& P, int precision, int src_kind, int dst
     return fast::edge_supported(P.nx) && fast::edge_supported(P.ny) && fast::edge_supported(P.nz);
 }
 
+namespace {
+
+// Arguments and launch geometry of one specialised apply.
 template <typename T>
-static cudaError_t fast_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
-    using T2 = c_t<T>;
+struct FastPlan {
     fast::FastArgs a{};
+    int xthreads = 0, stage_bytes = 0, xgrid_f = 0, xgrid_i = 0, zstages = 2, zgrid = 0;
+    size_t xsmem = 0, xismem = 0, zsmem = 0;
+    dim3 ygrid;
+    const CUtensorMap* smap = nullptr;
+    const CUtensorMap* gmap = nullptr;
+};
+
+template <typename T>
+cudaError_t fast_plan(Problem& P, const ApplyArgs& aa, FastPlan<T>& pl) {
+    using T2 = c_t<T>;
+    fast::FastArgs& a = pl.a;
+    a = fast::FastArgs{};
     a.nx = P.nx;
     a.ny = P.ny;
     a.nz = P.nz;
@@ -125,53 +139,118 @@ static cudaError_t fast_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
     if (rows > P.nrows) rows = (int)((P.nrows + 1) & ~1LL);
     a.rows = rows;
     a.ntiles = (P.nrows + rows - 1) / rows;
-    const int xthreads = ((3 * rows / 2 * fast::x_tpl(P.nx) + 31) / 32) * 32;
-    const size_t xsmem = (size_t)(3 * rows / 2) * fast::x_ld_rt<T>(P.nx) * sizeof(T2);
+    pl.xthreads = ((3 * rows / 2 * fast::x_tpl(P.nx) + 31) / 32) * 32;
+    pl.xsmem = (size_t)(3 * rows / 2) * fast::x_ld_rt<T>(P.nx) * sizeof(T2);
     // inverse x: two stages, each the raw half-spectrum rows of a tile or,
     // after stage A, its padded lines
     const size_t raw = (size_t)3 * rows * P.rs * sizeof(T2);
-    const int stage_bytes = (int)((std::max(raw, xsmem) + 15) & ~size_t(15));
-    const size_t xismem = 2 * (size_t)stage_bytes;
-    const int fwd_per_sm = fast::x_blocks_per_sm<T>(P.nx, false, xthreads, xsmem);
-    const int inv_per_sm = fast::x_blocks_per_sm<T>(P.nx, true, xthreads, xismem);
-    const int xgrid_f = (int)std::min<long long>(a.ntiles, (long long)fwd_per_sm * P.sm_count);
-    int xgrid_i = (int)std::min<long long>(a.ntiles, (long long)inv_per_sm * P.sm_count);
-    xgrid_i = std::min(xgrid_i, kMaxPartials);
+    pl.stage_bytes = (int)((std::max(raw, pl.xsmem) + 15) & ~size_t(15));
+    pl.xismem = 2 * (size_t)pl.stage_bytes;
+    const int fwd_per_sm = fast::x_blocks_per_sm<T>(P.nx, false, pl.xthreads, pl.xsmem);
+    const int inv_per_sm = fast::x_blocks_per_sm<T>(P.nx, true, pl.xthreads, pl.xismem);
+    pl.xgrid_f = (int)std::min<long long>(a.ntiles, (long long)fwd_per_sm * P.sm_count);
+    pl.xgrid_i = (int)std::min<long long>(a.ntiles, (long long)inv_per_sm * P.sm_count);
+    pl.xgrid_i = std::min(pl.xgrid_i, kMaxPartials);
 
     // y passes: TX kx columns of one z plane and one component per CTA
     constexpr int TX = fast::col_tx<T>();
     const int ntx = (P.nxh + TX - 1) / TX;
-    const dim3 ygrid(ntx, P.nz, 3);
+    pl.ygrid = dim3(ntx, P.nz, 3);
     // z pass: persistent, TMA-fed, two pipeline stages per CTA
     constexpr int TZ = fast::z_tx<T>();
-    const CUtensorMap* smap = nullptr;
-    const CUtensorMap* gmap = nullptr;
-    if (!fast_maps(P, sizeof(T) == 8, TZ, &smap, &gmap)) return cudaErrorNotSupported;
+    if (!fast_maps(P, sizeof(T) == 8, TZ, &pl.smap, &pl.gmap)) return cudaErrorNotSupported;
     // the tuning flag of the register-capped y/z kernels selects here the
     // single-stage z pass (three CTAs per SM instead of one two-stage CTA)
-    const int zstages = P.yz_lowreg ? 1 : 2;
-    const size_t zsmem = fast::z_smem_rt<T>(P.nz, zstages);
+    pl.zstages = P.yz_lowreg ? 1 : 2;
+    pl.zsmem = fast::z_smem_rt<T>(P.nz, pl.zstages);
     const int ntz = (P.nxh + TZ - 1) / TZ;
-    const int zgrid = (int)std::min<long long>(
+    pl.zgrid = (int)std::min<long long>(
         (long long)ntz * P.ny,
-        (long long)fast::z_blocks_per_sm<T>(P.nz, zstages, zsmem) * P.sm_count);
-
-    cudaStream_t st = P.stream;
-    cudaError_t e;
-    if ((e = fast::run_xfwd<T>(P.nx, a, xgrid_f, xthreads, xsmem, st)) != cudaSuccess) return e;
-    if ((e = fast::run_y<T>(P.ny, -1, a, ygrid, st)) != cudaSuccess) return e;
-    if ((e = fast::run_z<T>(P.nz, zstages, *smap, *gmap, a, dim3(zgrid), zsmem, st)) != cudaSuccess)
-        return e;
-    if ((e = fast::run_y<T>(P.ny, +1, a, ygrid, st)) != cudaSuccess) return e;
-    if ((e = fast::run_xinv<T>(P.nx, a, stage_bytes, xgrid_i, xthreads, xismem, st)) != cudaSuccess)
-        return e;
-    *nparts = xgrid_i;
+        (long long)fast::z_blocks_per_sm<T>(P.nz, pl.zstages, pl.zsmem) * P.sm_count);
     return cudaSuccess;
 }
+
+// The five passes; `members` > 1 launches the group kernels (a.group set):
+// the x passes keep each member's own grid (its partial sums are then the
+// same as in a single apply), the persistent z pass shares the resident
+// CTAs among the members.
+template <typename T>
+cudaError_t fast_run(const Problem& P, const FastPlan<T>& pl, const fast::FastArgs& a, int members) {
+    const unsigned G = (unsigned)members;
+    const int zgrid = members > 1 ? std::max(1, (pl.zgrid + members - 1) / members) : pl.zgrid;
+    cudaStream_t st = P.stream;
+    cudaError_t e;
+    if ((e = fast::run_xfwd<T>(P.nx, a, dim3(pl.xgrid_f, G), pl.xthreads, pl.xsmem, st)) != cudaSuccess)
+        return e;
+    const dim3 yg(pl.ygrid.x, pl.ygrid.y, 3 * G);
+    if ((e = fast::run_y<T>(P.ny, -1, a, yg, st)) != cudaSuccess) return e;
+    if ((e = fast::run_z<T>(P.nz, pl.zstages, *pl.smap, *pl.gmap, a, dim3(zgrid, G), pl.zsmem, st)) !=
+        cudaSuccess)
+        return e;
+    if ((e = fast::run_y<T>(P.ny, +1, a, yg, st)) != cudaSuccess) return e;
+    return fast::run_xinv<T>(P.nx, a, pl.stage_bytes, dim3(pl.xgrid_i, G), pl.xthreads, pl.xismem, st);
+}
+
+template <typename T>
+cudaError_t fast_impl(Problem& P, const ApplyArgs& aa, int* nparts) {
+    FastPlan<T> pl;
+    cudaError_t e = fast_plan<T>(P, aa, pl);
+    if (e != cudaSuccess) return e;
+    if ((e = fast_run<T>(P, pl, pl.a, 1)) != cudaSuccess) return e;
+    *nparts = pl.xgrid_i;
+    return cudaSuccess;
+}
+
+template <typename T>
+cudaError_t member_impl(Problem& P, const ApplyArgs& aa, fast::FastArgs* args, CUtensorMap* maps,
+                        long long* geometry) {
+    FastPlan<T> pl;
+    cudaError_t e = fast_plan<T>(P, aa, pl);
+    if (e != cudaSuccess) return e;
+    *args = pl.a;
+    maps[0] = *pl.smap;
+    maps[1] = *pl.gmap;
+    const long long g[kGroupGeometry] = {P.nx, P.ny, P.nz, pl.a.rows, pl.xthreads, pl.stage_bytes,
+                                         pl.xgrid_f, pl.xgrid_i, pl.zstages, (long long)pl.zsmem,
+                                         pl.zgrid, P.rs};
+    for (int i = 0; i < kGroupGeometry; ++i) geometry[i] = g[i];
+    return cudaSuccess;
+}
+
+template <typename T>
+cudaError_t group_impl(Problem& P0, int members, const fast::FastArgs* d_args, const CUtensorMap* d_maps,
+                       int* nparts) {
+    FastPlan<T> pl;
+    ApplyArgs aa;
+    cudaError_t e = fast_plan<T>(P0, aa, pl);
+    if (e != cudaSuccess) return e;
+    fast::FastArgs a = pl.a;
+    a.group = d_args;
+    a.group_maps = d_maps;
+    if ((e = fast_run<T>(P0, pl, a, members)) != cudaSuccess) return e;
+    *nparts = pl.xgrid_i;
+    return cudaSuccess;
+}
+
+}  // namespace
 
 cudaError_t fast_apply(Problem& P, int precision, const ApplyArgs& aa, int* nparts) {
     if (precision == kFP64) return fast_impl<double>(P, aa, nparts);
     return fast_impl<float>(P, aa, nparts);
+}
+
+cudaError_t fast_member_args(Problem& P, int precision, const ApplyArgs& aa, fast::FastArgs* args,
+                             CUtensorMap* maps, long long* geometry) {
+    if (!fast_apply_supported(P, precision, aa.src_kind, aa.dst_kind, aa.stage))
+        return cudaErrorNotSupported;
+    if (precision == kFP64) return member_impl<double>(P, aa, args, maps, geometry);
+    return member_impl<float>(P, aa, args, maps, geometry);
+}
+
+cudaError_t fast_apply_group(Problem& P0, int precision, int members, const fast::FastArgs* d_args,
+                             const CUtensorMap* d_maps, int* nparts) {
+    if (precision == kFP64) return group_impl<double>(P0, members, d_args, d_maps, nparts);
+    return group_impl<float>(P0, members, d_args, d_maps, nparts);
 }
 
 }  // namespace fp

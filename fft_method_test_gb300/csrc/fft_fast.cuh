@@ -285,6 +285,12 @@ struct FastArgs {
     double scale;
     double* partials;
     const int* skip;
+    // A group of problems of one grid in one launch per pass: when set, the
+    // kernels (GROUP = true) take their member's arguments from group[p], p =
+    // blockIdx.y (x and z passes) or blockIdx.z / 3 (y pass), and the z pass
+    // its tensor maps from group_maps[2p] (spectral) and [2p + 1] (Green).
+    const FastArgs* group;
+    const CUtensorMap* group_maps;
 };
 
 template <typename T>
@@ -333,8 +339,9 @@ __device__ __forceinline__ void store_pair(double2* p, double2 a, double2 b) {
     p[1] = b;
 }
 
-template <typename T, int N>
-__global__ void __launch_bounds__(384) k_fx_fwd(FastArgs a) {
+template <typename T, int N, bool GROUP>
+__global__ void __launch_bounds__(384) k_fx_fwd(const __grid_constant__ FastArgs a0) {
+    const FastArgs& a = GROUP ? a0.group[blockIdx.y] : a0;
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
     constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = Split<N>::TPL;
@@ -436,8 +443,9 @@ __global__ void __launch_bounds__(384) k_fx_fwd(FastArgs a) {
 // lines Z = A + iB of two real lines straight from the raw Hermitian half
 // spectra ([comp][row][rs], as copied); after a barrier the padded lines
 // overwrite the same stage.  stage_bytes covers the larger of the two layouts.
-template <typename T, int N>
-__global__ void __launch_bounds__(384) k_fx_inv(FastArgs a, int stage_bytes) {
+template <typename T, int N, bool GROUP>
+__global__ void __launch_bounds__(384) k_fx_inv(const __grid_constant__ FastArgs a0, int stage_bytes) {
+    const FastArgs& a = GROUP ? a0.group[blockIdx.y] : a0;
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
     constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = Split<N>::TPL;
@@ -554,9 +562,12 @@ __global__ void __launch_bounds__(384) k_fx_inv(FastArgs a, int stage_bytes) {
 
 // ---- P2 / P4: y pass -------------------------------------------------------------
 
-// One CTA: TX kx columns of one z plane for one component (blockIdx.z).
-template <typename T, int N, int S, int TX>
-__global__ void __launch_bounds__(TX * Split<N>::TPL) k_fcol_y(FastArgs a) {
+// One CTA: TX kx columns of one z plane for one component (blockIdx.z, or
+// blockIdx.z mod 3 of member blockIdx.z / 3 in a group).
+template <typename T, int N, int S, int TX, bool GROUP>
+__global__ void __launch_bounds__(TX * Split<N>::TPL) k_fcol_y(const __grid_constant__ FastArgs a0) {
+    const FastArgs& a = GROUP ? a0.group[blockIdx.z / 3] : a0;
+    const int comp = GROUP ? (int)(blockIdx.z % 3) : (int)blockIdx.z;
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
     constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = Split<N>::TPL;
@@ -567,7 +578,7 @@ __global__ void __launch_bounds__(TX * Split<N>::TPL) k_fcol_y(FastArgs a) {
     const int k0 = blockIdx.x * TX;
     const bool act = k0 + c < a.nxh;
     const T2* tw = tw_of<T>(a, 1);
-    T2* base = reinterpret_cast<T2*>(a.spec) + blockIdx.z * a.nh + (long long)blockIdx.y * N * a.rs +
+    T2* base = reinterpret_cast<T2*>(a.spec) + comp * a.nh + (long long)blockIdx.y * N * a.rs +
                k0 + (act ? c : 0);
     const long long es = a.rs;
     T2* my = lines + c * LD;
@@ -618,10 +629,13 @@ __host__ __device__ constexpr size_t z_stage_bytes() {
 // that touch one component only synchronise that component's threads (named
 // barrier 1 + comp); the Green multiply reads all three.  Waits are bounded:
 // on a timeout the CTA raises a.err and returns.
-template <typename T, int N, int TX, int STAGES>
+template <typename T, int N, int TX, int STAGES, bool GROUP>
 __global__ void __launch_bounds__(3 * TX * Split<N>::TPL, STAGES == 1 ? 3 : 1)
     k_fz(const __grid_constant__ CUtensorMap spec_map, const __grid_constant__ CUtensorMap green_map,
-         FastArgs a) {
+         const __grid_constant__ FastArgs a0) {
+    const FastArgs& a = GROUP ? a0.group[blockIdx.y] : a0;
+    const CUtensorMap* smap = GROUP ? &a0.group_maps[2 * blockIdx.y] : &spec_map;
+    const CUtensorMap* gmap = GROUP ? &a0.group_maps[2 * blockIdx.y + 1] : &green_map;
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
     constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = Split<N>::TPL;
@@ -646,6 +660,10 @@ __global__ void __launch_bounds__(3 * TX * Split<N>::TPL, STAGES == 1 ? 3 : 1)
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
         fence_mbar_init();
+        if (GROUP) {
+            fence_tensormap_acquire(smap);
+            fence_tensormap_acquire(gmap);
+        }
     }
     __syncthreads();
 
@@ -655,10 +673,9 @@ __global__ void __launch_bounds__(3 * TX * Split<N>::TPL, STAGES == 1 ? 3 : 1)
         const int ky = (int)(tile / ntx);
         mbar_arrive_expect_tx(&bars[st], TILE_BYTES);
         for (int cc = 0; cc < 3; ++cc)
-            tma_load_4d(base + (size_t)cc * CS * sizeof(T2), &spec_map, 2 * k0, ky, 0, cc, &bars[st]);
+            tma_load_4d(base + (size_t)cc * CS * sizeof(T2), smap, 2 * k0, ky, 0, cc, &bars[st]);
         for (int gc = 0; gc < 6; ++gc)
-            tma_load_4d(base + GOFF + (size_t)gc * N * TX * sizeof(T), &green_map, k0, ky, 0, gc,
-                        &bars[st]);
+            tma_load_4d(base + GOFF + (size_t)gc * N * TX * sizeof(T), gmap, k0, ky, 0, gc, &bars[st]);
     };
 
     long long tile = blockIdx.x;
@@ -738,6 +755,18 @@ __global__ void __launch_bounds__(3 * TX * Split<N>::TPL, STAGES == 1 ? 3 : 1)
 bool fast_apply_supported(const Problem& P, int precision, int src_kind, int dst_kind, int stage);
 cudaError_t fast_apply(Problem& P, int precision, const ApplyArgs& aa, int* nparts);
 
+// Group applies (one launch per pass for several problems of one grid and
+// tiling).  fast_member_args fills one member's kernel arguments, its two
+// tensor maps (spectral, Green) and the launch geometry the members of a
+// group must share (kGroupGeometry values); fast_apply_group launches the five
+// passes over `members` members whose arguments and maps the caller copied to
+// device memory (d_args[members], d_maps[2 * members], 64-byte aligned).
+constexpr int kGroupGeometry = 12;
+cudaError_t fast_member_args(Problem& P, int precision, const ApplyArgs& aa, fast::FastArgs* args,
+                             CUtensorMap* maps, long long* geometry);
+cudaError_t fast_apply_group(Problem& P0, int precision, int members, const fast::FastArgs* d_args,
+                             const CUtensorMap* d_maps, int* nparts);
+
 }  // namespace fp
 
 // ---- launch runners (fast32.cu / fast64.cu) -------------------------------------
@@ -807,10 +836,12 @@ size_t z_smem_rt(int n, int stages) {
 // Launch runners of one edge, defined in fast_runners.cuh and instantiated
 // per precision and edge group (fast32.cu, fast64.cu: powers of two;
 // fast32n.cu, fast64n.cu: 48, 80, 96, 160) so that they build in parallel.
+// A set a.group selects the group kernels; the grid then carries the member
+// index (grid.y for the x and z passes, grid.z = 3 x members for the y pass).
 template <typename T, int N>
 struct Passes {
-    static cudaError_t xfwd(const FastArgs& a, int grid, int threads, size_t smem, cudaStream_t s);
-    static cudaError_t xinv(const FastArgs& a, int stage_bytes, int grid, int threads, size_t smem,
+    static cudaError_t xfwd(const FastArgs& a, dim3 grid, int threads, size_t smem, cudaStream_t s);
+    static cudaError_t xinv(const FastArgs& a, int stage_bytes, dim3 grid, int threads, size_t smem,
                             cudaStream_t s);
     static cudaError_t y(int dir, const FastArgs& a, dim3 grid, cudaStream_t s);
     static cudaError_t z(int stages, const CUtensorMap& spec_map, const CUtensorMap& green_map,
@@ -821,9 +852,9 @@ struct Passes {
 };
 
 template <typename T>
-cudaError_t run_xfwd(int n, const FastArgs& a, int grid, int threads, size_t smem, cudaStream_t s);
+cudaError_t run_xfwd(int n, const FastArgs& a, dim3 grid, int threads, size_t smem, cudaStream_t s);
 template <typename T>
-cudaError_t run_xinv(int n, const FastArgs& a, int stage_bytes, int grid, int threads, size_t smem,
+cudaError_t run_xinv(int n, const FastArgs& a, int stage_bytes, dim3 grid, int threads, size_t smem,
                      cudaStream_t s);
 template <typename T>
 cudaError_t run_y(int n, int dir, const FastArgs& a, dim3 grid, cudaStream_t s);

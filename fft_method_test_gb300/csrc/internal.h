@@ -240,6 +240,44 @@ struct ApplyArgs {
 // of partial rows in *nparts.
 cudaError_t launch_apply(Problem& P, const ApplyArgs& a, int* nparts);
 
+// ---- groups of problems of one grid (kernels_minres.cu, group.cu) ----
+// One member's pointers for one MINRES iteration of a group: the group
+// kernels read tab[member] and run the same arithmetic as the single ones.
+struct IterArgs {
+    MinresScalars* sc;
+    double* partials;  // the apply's partial rows in, the vector kernels' out
+    int nparts;        // partial rows the apply wrote
+    int nblk;          // vector-kernel blocks of this member
+    double inv_nb;
+    long long nb;
+    double* z;
+    const double* v;
+    const double* v_old;
+    double* v_new;
+    double* w_prev;
+    const double* w;
+    double* x;
+    unsigned int* tickets;  // [0] z update, [1] v/w update
+    double* hist;
+};
+// Arguments of the next iteration of P (the buffer rotation at P.queued, which
+// it advances) and the apply it starts with.
+cudaError_t iteration_args(Problem& P, IterArgs* t, ApplyArgs* aa);
+// alpha, z update (+ Givens step), v/w/x update (+ iteration end) of
+// `members` problems, one launch each; max_blocks = the largest nblk.
+cudaError_t group_iteration_tail(cudaStream_t s, const IterArgs* d_tab, int members, int max_blocks);
+
+// Device tables of a group's lockstep iterations (group.cu).
+struct GroupTables;
+cudaError_t group_tables_create(GroupTables** out, int members, int iters);
+void group_tables_destroy(GroupTables* t);
+// true when P can be a group member (its applies run the specialised passes)
+bool group_supported(Problem& P);
+// `count` MINRES iterations of members m[0..members) in lockstep: per
+// iteration five pass launches and three vector-kernel launches for all of
+// them.  The members share grid, precision, tiling and stream (m[0]'s).
+cudaError_t group_iterations(Problem* const* m, int members, int count, GroupTables* t);
+
 // ---- vector kernels (kernels_minres.cu) ----
 cudaError_t launch_sum3(Problem& P, const double* v, long long nb, double* out3);
 // Reduce [nparts][4] partials into out4 (deterministic, one block).

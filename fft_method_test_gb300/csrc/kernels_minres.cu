@@ -83,8 +83,8 @@ __global__ void k_reduce4(const double* __restrict__ partials, int nparts, doubl
 
 // ---- iteration kernels ------------------------------------------------------
 
-__global__ void k_alpha(MinresScalars* sc, const double* __restrict__ partials, int nparts,
-                        double inv_nb) {
+__device__ __forceinline__ void alpha_body(MinresScalars* sc, const double* __restrict__ partials,
+                                           int nparts, double inv_nb) {
     if (sc->done) return;
     __shared__ double red[4 * 32];
     double acc[4] = {0, 0, 0, 0};
@@ -102,18 +102,25 @@ __global__ void k_alpha(MinresScalars* sc, const double* __restrict__ partials, 
     }
 }
 
+__global__ void k_alpha(MinresScalars* sc, const double* __restrict__ partials, int nparts,
+                        double inv_nb) {
+    alpha_body(sc, partials, nparts, inv_nb);
+}
+
 __device__ void scalar_step(MinresScalars* sc, const double* __restrict__ partials, int nparts,
                             double* hist, double* red);
 __device__ void finish_step(MinresScalars* sc, const double* __restrict__ partials, int nparts,
                             double* red);
-__device__ __forceinline__ bool last_block(unsigned int* counter);
+__device__ __forceinline__ bool last_block(unsigned int* counter, unsigned int nblk);
 
 // Two voxels (six doubles, three aligned double2) per thread: components are
 // static, loads are 16-byte vectors.  The odd tail voxel is handled by the
 // first thread of block 0.
-__global__ void k_zupd(MinresScalars* sc, double* __restrict__ z, const double* __restrict__ v,
-                       const double* __restrict__ v_old, long long nb, double* partials,
-                       unsigned int* counter, double* hist) {
+// blk / nblk: this block and the block count of the member's vector kernels
+__device__ __forceinline__ void zupd_body(MinresScalars* sc, double* __restrict__ z,
+                                          const double* __restrict__ v, const double* __restrict__ v_old,
+                                          long long nb, double* partials, unsigned int* counter,
+                                          double* hist, unsigned int blk, unsigned int nblk) {
     if (sc->done) return;
     __shared__ double red[32];
     const double alpha = sc->alpha, beta = sc->beta;
@@ -123,8 +130,8 @@ __global__ void k_zupd(MinresScalars* sc, double* __restrict__ z, const double* 
     double2* z2 = reinterpret_cast<double2*>(z);
     const double2* v2 = reinterpret_cast<const double2*>(v);
     const double2* o2 = reinterpret_cast<const double2*>(v_old);
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < npair;
-         k += (long long)gridDim.x * blockDim.x) {
+    for (long long k = (long long)blk * blockDim.x + threadIdx.x; k < npair;
+         k += (long long)nblk * blockDim.x) {
 #pragma unroll
         for (int h = 0; h < 3; ++h) {
             const double2 zz = z2[3 * k + h], vv = v2[3 * k + h], oo = o2[3 * k + h];
@@ -137,7 +144,7 @@ __global__ void k_zupd(MinresScalars* sc, double* __restrict__ z, const double* 
             acc[0] += a0 * a0 + a1 * a1;
         }
     }
-    if ((nb & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    if ((nb & 1) && blk == 0 && threadIdx.x == 0) {
         for (int c = 0; c < 3; ++c) {
             const long long i = 3 * (nb - 1) + c;
             const double a0 = z[i] - fma(beta, v_old[i], fma(alpha, v[i], mz[c]));
@@ -147,8 +154,14 @@ __global__ void k_zupd(MinresScalars* sc, double* __restrict__ z, const double* 
     }
     double o[1];
     block_sum<1>(acc, red, o);
-    if (threadIdx.x == 0) partials[blockIdx.x] = o[0];
-    if (last_block(counter)) scalar_step(sc, partials, gridDim.x, hist, red);
+    if (threadIdx.x == 0) partials[blk] = o[0];
+    if (last_block(counter, nblk)) scalar_step(sc, partials, (int)nblk, hist, red);
+}
+
+__global__ void k_zupd(MinresScalars* sc, double* __restrict__ z, const double* __restrict__ v,
+                       const double* __restrict__ v_old, long long nb, double* partials,
+                       unsigned int* counter, double* hist) {
+    zupd_body(sc, z, v, v_old, nb, partials, counter, hist, blockIdx.x, gridDim.x);
 }
 
 // The Givens step of one iteration from the |z|^2 partials, run by one whole
@@ -201,10 +214,12 @@ __device__ void scalar_step(MinresScalars* sc, const double* __restrict__ partia
     }
 }
 
-__global__ void k_vwupd(MinresScalars* sc, const double* __restrict__ z, const double* __restrict__ v,
-                        double* __restrict__ v_new, double* __restrict__ w_prev_to_next,
-                        const double* __restrict__ w, double* __restrict__ x, long long nb,
-                        double* partials, unsigned int* counter) {
+__device__ __forceinline__ void vwupd_body(MinresScalars* sc, const double* __restrict__ z,
+                                           const double* __restrict__ v, double* __restrict__ v_new,
+                                           double* __restrict__ w_prev_to_next,
+                                           const double* __restrict__ w, double* __restrict__ x,
+                                           long long nb, double* partials, unsigned int* counter,
+                                           unsigned int blk, unsigned int nblk) {
     if (sc->done) return;
     __shared__ double red[4 * 32];
     const double beta_new = sc->beta_new, eps = sc->eps, delta = sc->delta, rho = sc->rho;
@@ -224,8 +239,8 @@ __global__ void k_vwupd(MinresScalars* sc, const double* __restrict__ z, const d
     double2* wp2 = reinterpret_cast<double2*>(w_prev_to_next);
     const double2* w2 = reinterpret_cast<const double2*>(w);
     double2* x2 = reinterpret_cast<double2*>(x);
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < npair;
-         k += (long long)gridDim.x * blockDim.x) {
+    for (long long k = (long long)blk * blockDim.x + threadIdx.x; k < npair;
+         k += (long long)nblk * blockDim.x) {
 #pragma unroll
         for (int h = 0; h < 3; ++h) {
             const long long q = 3 * k + h;
@@ -241,7 +256,7 @@ __global__ void k_vwupd(MinresScalars* sc, const double* __restrict__ z, const d
             acc[(2 * h + 1) % 3] += vn1;
         }
     }
-    if ((nb & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    if ((nb & 1) && blk == 0 && threadIdx.x == 0) {
         for (int c = 0; c < 3; ++c) {
             const long long i = 3 * (nb - 1) + c;
             const double vo = v[i];
@@ -256,8 +271,35 @@ __global__ void k_vwupd(MinresScalars* sc, const double* __restrict__ z, const d
     double o[4];
     block_sum<4>(acc, red, o);
     if (threadIdx.x == 0)
-        for (int j = 0; j < 4; ++j) partials[4LL * blockIdx.x + j] = o[j];
-    if (last_block(counter)) finish_step(sc, partials, gridDim.x, red);
+        for (int j = 0; j < 4; ++j) partials[4LL * blk + j] = o[j];
+    if (last_block(counter, nblk)) finish_step(sc, partials, (int)nblk, red);
+}
+
+__global__ void k_vwupd(MinresScalars* sc, const double* __restrict__ z, const double* __restrict__ v,
+                        double* __restrict__ v_new, double* __restrict__ w_prev_to_next,
+                        const double* __restrict__ w, double* __restrict__ x, long long nb,
+                        double* partials, unsigned int* counter) {
+    vwupd_body(sc, z, v, v_new, w_prev_to_next, w, x, nb, partials, counter, blockIdx.x, gridDim.x);
+}
+
+// ---- group kernels: one launch for several problems (tab[member]) ------------
+
+__global__ void k_alpha_g(const IterArgs* __restrict__ tab) {
+    const IterArgs& t = tab[blockIdx.x];
+    alpha_body(t.sc, t.partials, t.nparts, t.inv_nb);
+}
+
+__global__ void k_zupd_g(const IterArgs* __restrict__ tab) {
+    const IterArgs& t = tab[blockIdx.y];
+    if (blockIdx.x >= (unsigned)t.nblk) return;
+    zupd_body(t.sc, t.z, t.v, t.v_old, t.nb, t.partials, t.tickets, t.hist, blockIdx.x, t.nblk);
+}
+
+__global__ void k_vwupd_g(const IterArgs* __restrict__ tab) {
+    const IterArgs& t = tab[blockIdx.y];
+    if (blockIdx.x >= (unsigned)t.nblk) return;
+    vwupd_body(t.sc, t.z, t.v, t.v_new, t.w_prev, t.w, t.x, t.nb, t.partials, t.tickets + 1, blockIdx.x,
+               t.nblk);
 }
 
 // The end of one iteration, run by one whole block (the last block of
@@ -277,15 +319,15 @@ __device__ void finish_step(MinresScalars* sc, const double* __restrict__ partia
     }
 }
 
-// true in every thread of the block that finishes last among the kernel's
-// blocks (its partial sums are then all in memory); the counter is reset
-__device__ __forceinline__ bool last_block(unsigned int* counter) {
+// true in every thread of the block that finishes last among the nblk blocks
+// of one problem (its partial sums are then all in memory); the counter is reset
+__device__ __forceinline__ bool last_block(unsigned int* counter, unsigned int nblk) {
     __shared__ bool last;
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
         const unsigned int t = atomicAdd(counter, 1u);
-        last = t == gridDim.x - 1;
+        last = t == nblk - 1;
         if (last) *counter = 0u;
     }
     __syncthreads();
@@ -523,34 +565,56 @@ void release_graphs(Problem& P) {
     }
 }
 
-cudaError_t minres_iteration(Problem& P) {
+cudaError_t iteration_args(Problem& P, IterArgs* t, ApplyArgs* aa) {
     const long long k = P.queued++;
     double* v = P.d_v[k % 3];
-    double* v_old = P.d_v[(k + 2) % 3];
-    double* v_new = P.d_v[(k + 1) % 3];
-    double* w_prev = P.d_w[k % 2];
-    double* w = P.d_w[(k + 1) % 2];
+    *aa = ApplyArgs{};
+    aa->src = v;
+    aa->src_sum = &P.d_sc->vsum[0];
+    aa->dst = P.d_z;
+    aa->dot_with = v;
+    aa->src_kind = kSrcCompact;
+    aa->dst_kind = kDstCompact;
+    aa->skip = &P.d_sc->done;
+    t->sc = P.d_sc;
+    t->partials = P.d_partials;
+    t->nparts = 0;
+    t->nblk = vec_blocks(P, (P.nb + 1) / 2);
+    t->inv_nb = 1.0 / (double)P.nb;
+    t->nb = P.nb;
+    t->z = P.d_z;
+    t->v = v;
+    t->v_old = P.d_v[(k + 2) % 3];
+    t->v_new = P.d_v[(k + 1) % 3];
+    t->w_prev = P.d_w[k % 2];
+    t->w = P.d_w[(k + 1) % 2];
+    t->x = P.d_x;
+    t->tickets = reinterpret_cast<unsigned int*>(P.d_red + kTicketSlot);
+    t->hist = P.d_hist;
+    return cudaSuccess;
+}
+
+cudaError_t group_iteration_tail(cudaStream_t s, const IterArgs* d_tab, int members, int max_blocks) {
+    FP_LAUNCHED(); k_alpha_g<<<members, 512, 0, s>>>(d_tab);
+    FP_LAUNCHED(); k_zupd_g<<<dim3(max_blocks, members), kVecThreads, 0, s>>>(d_tab);
+    FP_LAUNCHED(); k_vwupd_g<<<dim3(max_blocks, members), kVecThreads, 0, s>>>(d_tab);
+    return cudaGetLastError();
+}
+
+cudaError_t minres_iteration(Problem& P) {
+    IterArgs t;
     ApplyArgs a;
-    a.src = v;
-    a.src_sum = &P.d_sc->vsum[0];
-    a.dst = P.d_z;
-    a.dot_with = v;
-    a.src_kind = kSrcCompact;
-    a.dst_kind = kDstCompact;
-    a.skip = &P.d_sc->done;
+    iteration_args(P, &t, &a);
     int nparts = 0;
     cudaError_t e = launch_apply(P, a, &nparts);
     if (e != cudaSuccess) return e;
-    const double inv_nb = 1.0 / (double)P.nb;
-    FP_LAUNCHED(); k_alpha<<<1, 512, 0, P.stream>>>(P.d_sc, P.d_partials, nparts, inv_nb);
-    const int blocks = vec_blocks(P, (P.nb + 1) / 2);
+    FP_LAUNCHED(); k_alpha<<<1, 512, 0, P.stream>>>(t.sc, t.partials, nparts, t.inv_nb);
     // the last block of k_zupd runs the Givens step, the last block of
     // k_vwupd the end of the iteration (block-count tickets in d_red)
-    unsigned int* tickets = reinterpret_cast<unsigned int*>(P.d_red + kTicketSlot);
-    FP_LAUNCHED(); k_zupd<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, P.d_z, v, v_old, P.nb, P.d_partials,
-                                                                tickets, P.d_hist);
-    FP_LAUNCHED(); k_vwupd<<<blocks, kVecThreads, 0, P.stream>>>(P.d_sc, P.d_z, v, v_new, w_prev, w, P.d_x, P.nb,
-                                                                 P.d_partials, tickets + 1);
+    FP_LAUNCHED(); k_zupd<<<t.nblk, kVecThreads, 0, P.stream>>>(t.sc, t.z, t.v, t.v_old, t.nb, t.partials,
+                                                                 t.tickets, t.hist);
+    FP_LAUNCHED(); k_vwupd<<<t.nblk, kVecThreads, 0, P.stream>>>(t.sc, t.z, t.v, t.v_new, t.w_prev, t.w, t.x,
+                                                                  t.nb, t.partials, t.tickets + 1);
     return cudaGetLastError();
 }
 

@@ -55,6 +55,15 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
     return false;
 }
 
+// Acquire fence for a tensor map that lives in global memory (copied there by
+// the host before the launch): later TMA copies through it see its contents,
+// not a stale copy of an earlier map at the same address.
+__device__ __forceinline__ void fence_tensormap_acquire(const CUtensorMap* map) {
+    asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"(
+                     reinterpret_cast<uint64_t>(map))
+                 : "memory");
+}
+
 // 4-D tiled TMA load global -> shared, completing on bar (transaction bytes).
 __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
                                             int c3, uint64_t* bar) {

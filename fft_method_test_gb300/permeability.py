@@ -491,10 +491,12 @@ def computePermeabilityTensorFixedPoint(ids: np.ndarray, fluid_id: int = 1, flui
 def batch_solve_permeability(masks, precision: str = "mixed", tol: float = 1e-7,
                              maxit: int = 20000, concurrency: int = 4, autotune: bool = True,
                              voxel_sizes=None, mu: float = 1.0, p_radius: int = 2,
-                             support_mode: int = 0):
-    """fp_batch_solve_permeability over a list of fluid masks (each (nz, ny, nx),
+                             support_mode: int = 0, max_group: int = 1):
+    """fp_batch_solve_grouped over a list of fluid masks (each (nz, ny, nx),
     sizes may differ): returns (K of shape (count, 3, 3), stats per problem
-    [3 dicts each], status codes)."""
+    [3 dicts each], status codes).  max_group = 1 solves each problem on its
+    own (fp_batch_solve_permeability); larger values solve up to that many
+    problems of one grid together, one launch per pass for the group."""
     lib = _capi.load()
     count = len(masks)
     arrs = [np.ascontiguousarray(m, dtype=np.uint8) for m in masks]
@@ -504,11 +506,11 @@ def batch_solve_permeability(masks, precision: str = "mixed", tol: float = 1e-7,
     K = np.zeros(9 * max(count, 1))
     stats = (_capi.SolverStats * (3 * max(count, 1)))()
     status = np.zeros(max(count, 1), dtype=np.int32)
-    rc = lib.fp_batch_solve_permeability(count, dims.ctypes.data, ptrs,
-                                         None if vs is None else vs.ctypes.data, float(mu),
-                                         int(p_radius), PRECISIONS[precision], int(support_mode),
-                                         float(tol), int(maxit), int(concurrency), int(autotune),
-                                         K, stats, status.ctypes.data)
+    rc = lib.fp_batch_solve_grouped(count, dims.ctypes.data, ptrs,
+                                    None if vs is None else vs.ctypes.data, float(mu),
+                                    int(p_radius), PRECISIONS[precision], int(support_mode),
+                                    float(tol), int(maxit), int(concurrency), int(autotune),
+                                    int(max_group), K, stats, status.ctypes.data)
     if rc != _capi.FP_OK:
         msg = lib.fp_batch_last_error().decode()
         if rc == _capi.FP_ERR_INVALID:
@@ -516,6 +518,25 @@ def batch_solve_permeability(masks, precision: str = "mixed", tol: float = 1e-7,
         raise _capi.FpError(rc, msg)
     st = [[stats[3 * i + c].as_dict() for c in range(3)] for i in range(count)]
     return K[: 9 * count].reshape(count, 3, 3), st, status[:count].tolist()
+
+
+def group_solve_permeability(problems, tol: float, maxit: int = 20000):
+    """fp_group_solve_permeability: K of several PermeabilityProblem objects of
+    one grid (geometry set) solved together, one launch per pass for all of
+    them.  Returns (K of shape (count, 3, 3), stats per problem [3 dicts])."""
+    lib = _capi.load()
+    count = len(problems)
+    hs = (C.c_void_p * max(count, 1))(*[p.handle.value for p in problems])
+    K = np.zeros(9 * max(count, 1))
+    stats = (_capi.SolverStats * (3 * max(count, 1)))()
+    rc = lib.fp_group_solve_permeability(count, hs, float(tol), int(maxit), K, stats)
+    if rc != _capi.FP_OK:
+        msg = "; ".join(lib.fp_last_error(p.handle).decode() for p in problems)
+        if rc == _capi.FP_ERR_INVALID:
+            raise ValueError(msg)
+        raise _capi.FpError(rc, msg)
+    st = [[stats[3 * i + c].as_dict() for c in range(3)] for i in range(count)]
+    return K[: 9 * count].reshape(count, 3, 3), st
 
 
 def write_fvel(path: str, velocity, porosity: float, viscosity: float, driving) -> None:

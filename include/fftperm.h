@@ -217,7 +217,26 @@ int fp_batch_solve_permeability(int count, const int* dims, const uint8_t* const
                                 const double* voxel_sizes, double mu, int p_radius, int precision,
                                 int support_mode, double tol, int64_t maxit, int concurrency,
                                 int autotune, double* K, fp_solver_stats* stats, int* status);
+/* The same batch cut into groups of up to max_group problems of one grid and
+ * voxel size, each solved with fp_group_solve_permeability (max_group = 1 is
+ * fp_batch_solve_permeability). */
+int fp_batch_solve_grouped(int count, const int* dims, const uint8_t* const* masks,
+                           const double* voxel_sizes, double mu, int p_radius, int precision,
+                           int support_mode, double tol, int64_t maxit, int concurrency, int autotune,
+                           int max_group, double* K, fp_solver_stats* stats, int* status);
 const char* fp_batch_last_error(void);
+
+/* K of several problems of one grid (same dimensions, precision and reliable
+ * interval) solved together: the three load cases in turn, each as one
+ * lockstep MINRES over the members with one kernel launch per FFT pass and
+ * per vector kernel for all of them (no reference counterpart: the reference
+ * runs PermeabilityRunner::run once per geometry, src/app/PermeabilityRunner.cpp:451).
+ * Every member computes exactly what fp_solve_permeability computes for it.
+ * Members run on handles[0]'s stream for the duration.  When a member's grid
+ * has no specialised passes the members are solved one after another.
+ * K: count x 9 (row-major per member); stats: count x 3 or NULL. */
+int fp_group_solve_permeability(int count, fp_handle* handles, double tol, int64_t maxit, double* K,
+                                fp_solver_stats* stats);
 
 /* ---- learned warm start kernels (no reference counterpart) ------------------- */
 /* Building blocks of the warm-start network, all device pointers, queued on
