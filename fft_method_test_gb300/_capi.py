@@ -38,7 +38,7 @@ EXPORTED = [
     "fp_brinkman_permeability", "fp_brinkman_last_error", "fp_green_apply_noalloc",
     "fp_kernel_launch_count", "fp_brinkman_fft_solve", "fp_brinkman_fft_permeability",
     "fp_autotune", "fp_set_tiling", "fp_batch_solve_permeability", "fp_batch_solve_grouped",
-    "fp_group_solve_permeability", "fp_batch_last_error", "fp_write_fvel",
+    "fp_group_solve_permeability", "fp_solve_permeability_block", "fp_batch_last_error", "fp_write_fvel",
     "fp_nn_conv", "fp_nn_wgrad", "fp_nn_bias_grad", "fp_nn_relu_back", "fp_nn_adam", "fp_nn_loss",
     "fp_measure_fp64_rate", "fp_nn_conv_tc", "fp_nn_tc_error", "fp_nn_pool2", "fp_nn_pool2_back",
     "fp_nn_up2_add", "fp_nn_up2_add_back", "fp_nn_wgrad_cc", "fp_time_apply",
@@ -130,6 +130,7 @@ _SIGNATURES = {
                                 C.c_int, C.c_int, _dp, C.c_void_p, C.c_void_p], C.c_int),
     "fp_group_solve_permeability": ([C.c_int, C.c_void_p, C.c_double, C.c_int64, _dp, C.c_void_p],
                                      C.c_int),
+    "fp_solve_permeability_block": ([_h, C.c_double, C.c_int64, _dp, C.POINTER(SolverStats)], C.c_int),
     "fp_batch_last_error": ([], C.c_char_p),
     "fp_nn_conv": ([C.c_int, C.c_int, C.c_int, C.c_int64, C.c_int, C.c_int, C.c_void_p, C.c_int,
                     C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p],

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -1003,6 +1004,70 @@ int fp_solve_permeability(fp_handle h, double tol, int64_t maxit, double K[9],
     return FP_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Member i solves load case cols[i] (unit gradient e_col); the members run
+// on handles[0]'s stream and iterate in lockstep (group_minres).  avg[i] is
+// the member's domain-averaged velocity, st[i] its solver statistics.
+int group_solve_cases(int count, fp_handle* handles, const int* cols, double tol, long long maxit,
+                      double (*avg)[3], fp_solver_stats* st) {
+    Problem& P0 = handles[0]->P;
+    std::vector<cudaStream_t> own((size_t)count);
+    for (int i = 0; i < count; ++i) {
+        Problem& P = handles[i]->P;
+        own[(size_t)i] = P.stream;
+        FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
+        P.stream = P0.stream;
+    }
+    fp::GroupTables* tab = nullptr;
+    auto restore = [&](int rc) {
+        cudaStreamSynchronize(P0.stream);
+        for (int i = 0; i < count; ++i) handles[i]->P.stream = own[(size_t)i];
+        fp::group_tables_destroy(tab);
+        return rc;
+    };
+    const int chunk = P0.precision == fp::kMixed && P0.reliable_interval > 0 ? P0.reliable_interval : 16;
+    {
+        cudaError_t e = fp::group_tables_create(&tab, count, chunk);
+        if (e != cudaSuccess) return restore(cuda_fail(P0, e, "group tables"));
+    }
+    const double t0 = now_s();
+    std::vector<MinresRun> runs((size_t)count);
+    for (int i = 0; i < count; ++i) {
+        Problem& P = handles[i]->P;
+        double g[3] = {0.0, 0.0, 0.0};
+        g[cols[i]] = 1.0;
+        int rc = device_build_rhs(P, g, P.d_b);
+        if (!rc) rc = minres_begin(runs[(size_t)i], P, P.d_b, nullptr, tol, maxit);
+        if (rc) return restore(rc);
+    }
+    int rc = group_minres(runs, tab);
+    if (rc) return restore(rc);
+    for (int i = 0; i < count; ++i) {
+        Problem& P = handles[i]->P;
+        double g[3] = {0.0, 0.0, 0.0};
+        g[cols[i]] = 1.0;
+        st[i] = fp_solver_stats{};
+        rc = minres_finish(runs[(size_t)i], nullptr, &st[i]);
+        if (!rc) rc = device_recover(P, g, P.d_x, avg[i], false);
+        if (rc) return restore(rc);
+        st[i].seconds = now_s() - t0;
+    }
+    return restore(FP_OK);
+}
+
+// colK = -mu <v>; set_column stores -colK (PermeabilityRunner.cpp:772-777,
+// PermeabilityTensor.cpp:16)
+void set_column(double* K, int col, double mu, const double avg[3]) {
+    for (int row = 0; row < 3; ++row) K[row * 3 + col] = -(-mu * avg[row]);
+}
+
+}  // namespace
+
+extern "C" {
+
 int fp_group_solve_permeability(int count, fp_handle* handles, double tol, int64_t maxit, double* K,
                                 fp_solver_stats* stats) {
     if (count < 1 || !handles || !K) return FP_ERR_INVALID;
@@ -1027,54 +1092,90 @@ int fp_group_solve_permeability(int count, fp_handle* handles, double tol, int64
         }
         return FP_OK;
     }
-    // every member on the first member's stream for the duration
-    std::vector<cudaStream_t> own((size_t)count);
-    for (int i = 0; i < count; ++i) {
-        Problem& P = handles[i]->P;
-        own[(size_t)i] = P.stream;
-        FP_CUDA(cudaStreamSynchronize(P.stream), "sync");
-        P.stream = P0.stream;
-    }
-    fp::GroupTables* tab = nullptr;
-    auto restore = [&](int rc) {
-        cudaStreamSynchronize(P0.stream);
-        for (int i = 0; i < count; ++i) handles[i]->P.stream = own[(size_t)i];
-        fp::group_tables_destroy(tab);
-        return rc;
-    };
-    const int chunk = P0.precision == fp::kMixed && P0.reliable_interval > 0 ? P0.reliable_interval : 16;
-    {
-        cudaError_t e = fp::group_tables_create(&tab, count, chunk);
-        if (e != cudaSuccess) return restore(cuda_fail(P0, e, "group tables"));
-    }
-    std::vector<MinresRun> runs((size_t)count);
+    std::vector<int> cols((size_t)count);
+    std::vector<std::array<double, 3>> avg((size_t)count);
+    std::vector<fp_solver_stats> st((size_t)count);
     for (int col = 0; col < 3; ++col) {
-        double g[3] = {0.0, 0.0, 0.0};
-        g[col] = 1.0;
-        const double t0 = now_s();
+        std::fill(cols.begin(), cols.end(), col);
+        int rc = group_solve_cases(count, handles, cols.data(), tol, maxit,
+                                   reinterpret_cast<double(*)[3]>(avg.data()), st.data());
+        if (rc) return rc;
         for (int i = 0; i < count; ++i) {
-            Problem& P = handles[i]->P;
-            int rc = device_build_rhs(P, g, P.d_b);
-            if (!rc) rc = minres_begin(runs[(size_t)i], P, P.d_b, nullptr, tol, maxit);
-            if (rc) return restore(rc);
-        }
-        int rc = group_minres(runs, tab);
-        if (rc) return restore(rc);
-        for (int i = 0; i < count; ++i) {
-            Problem& P = handles[i]->P;
-            fp_solver_stats st{};
-            rc = minres_finish(runs[(size_t)i], nullptr, &st);
-            double avg[3];
-            if (!rc) rc = device_recover(P, g, P.d_x, avg, false);
-            if (rc) return restore(rc);
-            // colK = -mu <v>; set_column stores -colK (PermeabilityRunner.cpp:772-777,
-            // PermeabilityTensor.cpp:16)
-            for (int row = 0; row < 3; ++row) K[9 * (size_t)i + row * 3 + col] = -(-P.mu * avg[row]);
-            st.seconds = now_s() - t0;
-            if (stats) stats[3 * (size_t)i + col] = st;
+            set_column(K + 9 * (size_t)i, col, handles[i]->P.mu, avg[(size_t)i].data());
+            if (stats) stats[3 * (size_t)i + col] = st[(size_t)i];
         }
     }
-    return restore(FP_OK);
+    return FP_OK;
+}
+
+int fp_solve_permeability_block(fp_handle h, double tol, int64_t maxit, double K[9],
+                                fp_solver_stats stats[3]) {
+    if (!h || !K) return FP_ERR_INVALID;
+    Problem& P = h->P;
+    int rc = need_geometry(P, "PermeabilityRunner::run");
+    if (rc) return rc;
+    if (!fp::group_supported(P)) return fp_solve_permeability(h, tol, maxit, K, stats);
+    // the Green tables the siblings borrow
+    rc = P.precision == fp::kMixed ? ensure_green_both(P) : ensure_green64(P);
+    if (rc) return rc;
+    // two siblings: own vectors, spectral buffer and scalars; the same mask,
+    // support, tiling and solver settings; the Green tables of h
+    fp_handle sib[2] = {nullptr, nullptr};
+    auto drop = [&](int code) {
+        for (fp_handle s : sib) {
+            if (!s) continue;
+            s->P.d_green32 = nullptr;  // borrowed
+            s->P.d_green64 = nullptr;
+            fp_destroy(s);
+        }
+        return code;
+    };
+    for (int k = 0; k < 2; ++k) {
+        rc = fp::create_handle(P.nx, P.ny, P.nz, P.h, P.mu, P.p_radius, P.precision, false, &sib[k]);
+        if (rc) {
+            if (sib[k]) P.err = "block solve: " + sib[k]->P.err;
+            return drop(rc);
+        }
+        Problem& S = sib[k]->P;
+        S.support_mode = P.support_mode;
+        S.reliable_interval = P.reliable_interval;
+        S.ahead_factor = P.ahead_factor;
+        S.segment_tol_factor = P.segment_tol_factor;
+        S.use_graphs = P.use_graphs;
+        S.fast_off = P.fast_off;
+        S.tma_off = P.tma_off;
+        S.x_bulk = P.x_bulk;
+        S.x_rows = P.x_rows;
+        S.tile_yz = P.tile_yz;
+        S.yz_lowreg = P.yz_lowreg;
+        cudaError_t e = cudaStreamSynchronize(P.stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(S.d_mask, P.d_mask, (size_t)P.n, cudaMemcpyDeviceToDevice, S.stream);
+        if (e != cudaSuccess) return drop(cuda_fail(P, e, "block solve: mask copy"));
+        rc = finish_geometry(S, nullptr);
+        if (!rc && S.nb != P.nb) rc = fail(S, FP_ERR_STATE, "support size differs");
+        if (rc) {
+            P.err = "block solve: " + S.err;
+            return drop(rc);
+        }
+        S.d_green32 = P.d_green32;
+        S.d_green64 = P.d_green64;
+    }
+    fp_handle members[3] = {h, sib[0], sib[1]};
+    const int cols[3] = {0, 1, 2};
+    double avg[3][3];
+    fp_solver_stats st[3];
+    rc = group_solve_cases(3, members, cols, tol, maxit, avg, st);
+    if (rc) {
+        for (fp_handle s : sib)
+            if (!s->P.err.empty()) P.err = "block solve: " + s->P.err;
+        return drop(rc);
+    }
+    for (int c = 0; c < 3; ++c) {
+        set_column(K, c, P.mu, avg[c]);
+        if (stats) stats[c] = st[c];
+    }
+    return drop(FP_OK);
 }
 
 }  // extern "C"

@@ -341,7 +341,10 @@ __device__ __forceinline__ void store_pair(double2* p, double2 a, double2 b) {
 
 template <typename T, int N, bool GROUP>
 __global__ void __launch_bounds__(384) k_fx_fwd(const __grid_constant__ FastArgs a0) {
-    const FastArgs& a = GROUP ? a0.group[blockIdx.y] : a0;
+    // a group member's arguments are copied out of the table once: read
+    // through a reference they would be reloaded after every global store
+    const FastArgs ag = GROUP ? a0.group[blockIdx.y] : FastArgs{};
+    const FastArgs& a = GROUP ? ag : a0;
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
     constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = Split<N>::TPL;
@@ -445,7 +448,8 @@ __global__ void __launch_bounds__(384) k_fx_fwd(const __grid_constant__ FastArgs
 // overwrite the same stage.  stage_bytes covers the larger of the two layouts.
 template <typename T, int N, bool GROUP>
 __global__ void __launch_bounds__(384) k_fx_inv(const __grid_constant__ FastArgs a0, int stage_bytes) {
-    const FastArgs& a = GROUP ? a0.group[blockIdx.y] : a0;
+    const FastArgs ag = GROUP ? a0.group[blockIdx.y] : FastArgs{};
+    const FastArgs& a = GROUP ? ag : a0;
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
     constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = Split<N>::TPL;
@@ -566,7 +570,8 @@ __global__ void __launch_bounds__(384) k_fx_inv(const __grid_constant__ FastArgs
 // blockIdx.z mod 3 of member blockIdx.z / 3 in a group).
 template <typename T, int N, int S, int TX, bool GROUP>
 __global__ void __launch_bounds__(TX * Split<N>::TPL) k_fcol_y(const __grid_constant__ FastArgs a0) {
-    const FastArgs& a = GROUP ? a0.group[blockIdx.z / 3] : a0;
+    const FastArgs ag = GROUP ? a0.group[blockIdx.z / 3] : FastArgs{};
+    const FastArgs& a = GROUP ? ag : a0;
     const int comp = GROUP ? (int)(blockIdx.z % 3) : (int)blockIdx.z;
     if (a.skip && *a.skip) return;
     using T2 = c_t<T>;
@@ -633,6 +638,8 @@ template <typename T, int N, int TX, int STAGES, bool GROUP>
 __global__ void __launch_bounds__(3 * TX * Split<N>::TPL, STAGES == 1 ? 3 : 1)
     k_fz(const __grid_constant__ CUtensorMap spec_map, const __grid_constant__ CUtensorMap green_map,
          const __grid_constant__ FastArgs a0) {
+    // (the few fields read per tile are read through the table: a copy would
+    // hold them in registers across the kernel)
     const FastArgs& a = GROUP ? a0.group[blockIdx.y] : a0;
     const CUtensorMap* smap = GROUP ? &a0.group_maps[2 * blockIdx.y] : &spec_map;
     const CUtensorMap* gmap = GROUP ? &a0.group_maps[2 * blockIdx.y + 1] : &green_map;

@@ -94,6 +94,18 @@ cudaError_t group_iterations(Problem* const* m, int members, int count, GroupTab
         else if (std::memcmp(geom0, g, sizeof(g)) != 0)
             return cudaErrorInvalidValue;
     }
+    // The Green table depends only on the grid, voxel size, viscosity and
+    // alias radius: members that share them all read member 0's table (one
+    // table in L2 for the group; at 256^3 the members' z passes run one after
+    // another, so this saves memory traffic only on small grids, where the
+    // members' z-pass CTAs are resident together).
+    for (int p = 1; p < members; ++p) {
+        const Problem& P = *m[p];
+        if (P.h == P0.h && P.mu == P0.mu && P.p_radius == P0.p_radius) {
+            base[(size_t)p].green = base[0].green;
+            t->h_maps[2 * p + 1] = t->h_maps[1];
+        }
+    }
     const int nparts = (int)geom0[7];  // partial rows of the inverse x pass
     int max_blocks = 1;
     for (int i = 0; i < count; ++i) {

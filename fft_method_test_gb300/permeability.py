@@ -247,10 +247,14 @@ class PermeabilityProblem:
                                                 C.byref(st)))
         return avg, st.as_dict(), xo
 
-    def solve_permeability(self, tol: float, maxit: int):
+    def solve_permeability(self, tol: float, maxit: int, block: bool = False):
+        """K from the three load cases (fp_solve_permeability), or with
+        block=True the three as one lockstep block (fp_solve_permeability_block;
+        the same K)."""
         K = np.zeros(9)
         stats = (_capi.SolverStats * 3)()
-        self._check(self.lib.fp_solve_permeability(self._h, float(tol), int(maxit), K, stats))
+        fn = self.lib.fp_solve_permeability_block if block else self.lib.fp_solve_permeability
+        self._check(fn(self._h, float(tol), int(maxit), K, stats))
         return K.reshape(3, 3), [s.as_dict() for s in stats]
 
 

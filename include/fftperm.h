@@ -238,6 +238,17 @@ const char* fp_batch_last_error(void);
 int fp_group_solve_permeability(int count, fp_handle* handles, double tol, int64_t maxit, double* K,
                                 fp_solver_stats* stats);
 
+/* fp_solve_permeability with the three load cases as one block (3-RHS): two
+ * sibling solves on the same support borrow h's Green tables, and the three
+ * load cases iterate in lockstep as a group (one launch per pass for the
+ * three fields; their z passes read one Green table, tile by tile at the
+ * same time).  Same K and statistics as fp_solve_permeability (each load
+ * case computes exactly what it computes alone); when h's grid has no
+ * specialised passes it is fp_solve_permeability.  Extra device memory: two
+ * sets of Krylov vectors and spectral buffers. */
+int fp_solve_permeability_block(fp_handle h, double tol, int64_t maxit, double K[9],
+                                fp_solver_stats stats[3]);
+
 /* ---- learned warm start kernels (no reference counterpart) ------------------- */
 /* Building blocks of the warm-start network, all device pointers, queued on
  * `stream` (cudaStream_t, NULL = legacy default).  Activations are

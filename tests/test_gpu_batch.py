@@ -222,3 +222,33 @@ def test_grouped_batch_fp64_matches_oracle(gpu_lib, restatement):
     for i, m in enumerate(masks):
         K_ref, _ = restatement.context(m).solve_permeability(1e-10, 6000)
         assert rel_err(K[i], K_ref) < 1e-9, i
+
+
+@pytest.mark.parametrize("n,precision,tol", [(32, "fp64", 1e-10), (48, "mixed", 1e-7),
+                                             (64, "mixed", 1e-7)])
+def test_block_solve_equals_load_cases_one_by_one(gpu_lib, n, precision, tol):
+    """fp_solve_permeability_block (three load cases in lockstep, one Green
+    table for the three) gives the K and iteration counts of
+    fp_solve_permeability exactly."""
+    from fft_method_test_gb300.permeability import PermeabilityProblem
+
+    mask = G.gaussian_field(n, 4.0, 0.4, seed=70 + n)
+    with PermeabilityProblem(mask.shape, precision=precision) as p:
+        p.set_geometry(mask)
+        K0, st0 = p.solve_permeability(tol, 20000)
+        K1, st1 = p.solve_permeability(tol, 20000, block=True)
+        K2, _ = p.solve_permeability(tol, 20000)  # the handle is unchanged after a block solve
+    assert np.array_equal(K0, K1), rel_err(K0, K1)
+    assert np.array_equal(K0, K2)
+    assert [s["iterations"] for s in st0] == [s["iterations"] for s in st1]
+
+
+def test_block_solve_on_unspecialised_grid(gpu_lib):
+    from fft_method_test_gb300.permeability import PermeabilityProblem
+
+    mask = G.gaussian_field(40, 4.0, 0.4, seed=77)
+    with PermeabilityProblem(mask.shape, precision="fp64") as p:
+        p.set_geometry(mask)
+        K0, _ = p.solve_permeability(1e-10, 20000)
+        K1, _ = p.solve_permeability(1e-10, 20000, block=True)
+    assert np.array_equal(K0, K1)
