@@ -59,6 +59,14 @@ cudaError_t run_z(int n, int stages, const CUtensorMap& spec_map, const CUtensor
 }
 
 template <typename T>
+cudaError_t run_z_shared(int n, const FastArgs& a, int grid, size_t smem, cudaStream_t s) {
+#define FP_CALL(N) Passes<T, N>::z_shared(a, grid, smem, s)
+    FP_EDGE_SWITCH(n, FP_CALL)
+#undef FP_CALL
+    return cudaErrorInvalidValue;
+}
+
+template <typename T>
 int z_blocks_per_sm(int n, int stages, size_t smem) {
 #define FP_CALL(N) Passes<T, N>::z_per_sm(stages, smem)
     FP_EDGE_SWITCH(n, FP_CALL)
@@ -185,9 +193,11 @@ cudaError_t fast_run(const Problem& P, const FastPlan<T>& pl, const fast::FastAr
         return e;
     const dim3 yg(pl.ygrid.x, pl.ygrid.y, 3 * G);
     if ((e = fast::run_y<T>(P.ny, -1, a, yg, st)) != cudaSuccess) return e;
-    if ((e = fast::run_z<T>(P.nz, pl.zstages, *pl.smap, *pl.gmap, a, dim3(zgrid, G), pl.zsmem, st)) !=
-        cudaSuccess)
-        return e;
+    if (members > 1 && a.share == members && pl.zstages == 2)
+        e = fast::run_z_shared<T>(P.nz, a, zgrid, pl.zsmem, st);
+    else
+        e = fast::run_z<T>(P.nz, pl.zstages, *pl.smap, *pl.gmap, a, dim3(zgrid, G), pl.zsmem, st);
+    if (e != cudaSuccess) return e;
     if ((e = fast::run_y<T>(P.ny, +1, a, yg, st)) != cudaSuccess) return e;
     return fast::run_xinv<T>(P.nx, a, pl.stage_bytes, dim3(pl.xgrid_i, G), pl.xthreads, pl.xismem, st);
 }
@@ -220,7 +230,7 @@ cudaError_t member_impl(Problem& P, const ApplyArgs& aa, fast::FastArgs* args, C
 
 template <typename T>
 cudaError_t group_impl(Problem& P0, int members, const fast::FastArgs* d_args, const CUtensorMap* d_maps,
-                       int* nparts) {
+                       bool shared_green, int* nparts) {
     FastPlan<T> pl;
     ApplyArgs aa;
     cudaError_t e = fast_plan<T>(P0, aa, pl);
@@ -228,6 +238,7 @@ cudaError_t group_impl(Problem& P0, int members, const fast::FastArgs* d_args, c
     fast::FastArgs a = pl.a;
     a.group = d_args;
     a.group_maps = d_maps;
+    a.share = shared_green ? members : 0;
     if ((e = fast_run<T>(P0, pl, a, members)) != cudaSuccess) return e;
     *nparts = pl.xgrid_i;
     return cudaSuccess;
@@ -249,9 +260,9 @@ cudaError_t fast_member_args(Problem& P, int precision, const ApplyArgs& aa, fas
 }
 
 cudaError_t fast_apply_group(Problem& P0, int precision, int members, const fast::FastArgs* d_args,
-                             const CUtensorMap* d_maps, int* nparts) {
-    if (precision == kFP64) return group_impl<double>(P0, members, d_args, d_maps, nparts);
-    return group_impl<float>(P0, members, d_args, d_maps, nparts);
+                             const CUtensorMap* d_maps, bool shared_green, int* nparts) {
+    if (precision == kFP64) return group_impl<double>(P0, members, d_args, d_maps, shared_green, nparts);
+    return group_impl<float>(P0, members, d_args, d_maps, shared_green, nparts);
 }
 
 }  // namespace fp

@@ -69,6 +69,13 @@ cudaError_t Passes<T, N>::z(int stages, const CUtensorMap& spec_map, const CUten
 }
 
 template <typename T, int N>
+cudaError_t Passes<T, N>::z_shared(const FastArgs& a, int grid, size_t smem, cudaStream_t s) {
+    constexpr int TX = z_tx<T>();
+    FP_RUN((k_fz_shared<T, N, TX>), grid, 3 * TX * Split<N>::TPL, smem, s, a);
+    return cudaGetLastError();
+}
+
+template <typename T, int N>
 int Passes<T, N>::z_per_sm(int stages, size_t smem) {
     constexpr int TX = z_tx<T>();
     static std::atomic<unsigned long long> f1{0}, f2{0};

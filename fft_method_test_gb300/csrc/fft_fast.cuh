@@ -291,6 +291,9 @@ struct FastArgs {
     // its tensor maps from group_maps[2p] (spectral) and [2p + 1] (Green).
     const FastArgs* group;
     const CUtensorMap* group_maps;
+    // members of a group whose z pass shares one Green table (group_maps[1]):
+    // k_fz_shared loads each Green tile once for all of them (0 = not shared)
+    int share;
 };
 
 template <typename T>
@@ -754,6 +757,129 @@ __global__ void __launch_bounds__(3 * TX * Split<N>::TPL, STAGES == 1 ? 3 : 1)
     }
 }
 
+// The z pass of a group whose members share one Green table (the three load
+// cases of one cell, or cells of one grid and Green parameters): each CTA
+// walks its (kx, ky) tiles and, per tile, the members one after another as
+// pipeline items (tile, member).  The spectral boxes of item i + 1 load into
+// the other stage while item i is transformed, as in k_fz; the Green tile is
+// loaded once per tile, with the tile's first item, into one of two Green
+// buffers (tile parity) and serves all members.  Per tile the HBM reads are
+// G spectral tiles and one Green tile instead of G of each (the byte model
+// of a G-field block apply).  A member whose solve is done is transformed
+// all the same (its spectrum is scratch that the next fresh apply rewrites).
+// Waits are bounded: on a timeout member 0's error flag is raised.
+template <typename T, int N, int TX>
+__global__ void __launch_bounds__(3 * TX * Split<N>::TPL, sizeof(T) == 4 ? 2 : 1)
+    k_fz_shared(const __grid_constant__ FastArgs a0) {
+    using T2 = c_t<T>;
+    constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, TPL = Split<N>::TPL;
+    constexpr int LD = col_ld<N, T, TX>();
+    constexpr int CS = comp_stride<T, N, TX>();
+    constexpr size_t SPEC = z_green_offset<T, N, TX>();  // one spectral stage (128-byte multiple)
+    constexpr size_t GREEN = ((size_t)6 * N * TX * sizeof(T) + 127) & ~size_t(127);
+    constexpr uint32_t SPEC_BYTES = (uint32_t)(3 * N * TX * sizeof(T2));
+    constexpr uint32_t GREEN_BYTES = (uint32_t)(6 * N * TX * sizeof(T));
+    static_assert(128 + 2 * SPEC + 2 * GREEN <= 128 + 2 * z_stage_bytes<T, N, TX>(), "shared memory");
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
+    unsigned char* spec0 = smem_raw + 128;
+    unsigned char* green0 = spec0 + 2 * SPEC;
+    const int G = a0.share;
+    int* err = a0.group[0].err;
+    const int c = threadIdx.x % TX;
+    const int t = (threadIdx.x / TX) % TPL;
+    const int comp = threadIdx.x / (TX * TPL);
+    using GBar = typename std::conditional<(TX * TPL) % 32 == 0, GroupBarrier, CtaBarrier>::type;
+    GBar gbar = make_group_barrier<GBar>(1 + comp, TX * TPL);
+    const int ntx = (a0.nxh + TX - 1) / TX;
+    const long long ntiles = (long long)ntx * a0.ny;
+    const T2* tw = tw_of<T>(a0, 2);
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+        fence_tensormap_acquire(&a0.group_maps[1]);
+        for (int m = 0; m < G; ++m) fence_tensormap_acquire(&a0.group_maps[2 * m]);
+    }
+    __syncthreads();
+    const long long my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const int nitems = (int)(my_tiles * G);
+
+    auto issue = [&](int i) {
+        const int st = i & 1;
+        const int m = i % G;
+        const long long tile = blockIdx.x + (long long)(i / G) * gridDim.x;
+        const int k0 = (int)(tile % ntx) * TX;
+        const int ky = (int)(tile / ntx);
+        unsigned char* sb = spec0 + st * SPEC;
+        mbar_arrive_expect_tx(&bars[st], SPEC_BYTES + (m == 0 ? GREEN_BYTES : 0u));
+        for (int cc = 0; cc < 3; ++cc)
+            tma_load_4d(sb + (size_t)cc * CS * sizeof(T2), &a0.group_maps[2 * m], 2 * k0, ky, 0, cc,
+                        &bars[st]);
+        if (m == 0) {
+            unsigned char* gb = green0 + ((i / G) & 1) * GREEN;
+            for (int gc = 0; gc < 6; ++gc)
+                tma_load_4d(gb + (size_t)gc * N * TX * sizeof(T), &a0.group_maps[1], k0, ky, 0, gc,
+                            &bars[st]);
+        }
+    };
+
+    if (threadIdx.x == 0 && nitems > 0) issue(0);
+    for (int i = 0; i < nitems; ++i) {
+        const int st = i & 1;
+        if (threadIdx.x == 0 && i + 1 < nitems) {
+            fence_proxy_async_smem();
+            issue(i + 1);
+        }
+        if (!tma_pipeline_wait<T2>(bars, i, st, i + 1 < nitems, err)) return;
+        const int m = i % G;
+        const long long tile = blockIdx.x + (long long)(i / G) * gridDim.x;
+        T2* blk = reinterpret_cast<T2*>(spec0 + st * SPEC);
+        const T* gsm = reinterpret_cast<const T*>(green0 + ((i / G) & 1) * GREEN);
+        const int k0 = (int)(tile % ntx) * TX;
+        const long long ky = tile / ntx;
+        const bool act = k0 + c < a0.nxh;
+        T2* my = blk + comp * CS + c * LD;
+        {
+            const T2* rc = blk + comp * CS + c;
+            auto ld_raw = [&](int pos) { return rc[pos * TX]; };
+            stage_a<R1, R2, -1, TPL, true>(my, t, act, tw, ld_raw, gbar);
+        }
+        gbar();
+        {
+            auto st_nat = [&](int pos, T2 v) { my[pos] = v; };
+            stage_b<R1, R2, -1, TPL, true>(my, t, act, st_nat, gbar);
+        }
+        __syncthreads();
+        {
+            const T2* lx = blk + 0 * CS + c * LD;
+            const T2* ly = blk + 1 * CS + c * LD;
+            const T2* lz = blk + 2 * CS + c * LD;
+            const int g0 = comp == 0 ? 0 : (comp == 1 ? 1 : 2);
+            const int g1 = comp == 0 ? 1 : (comp == 1 ? 3 : 4);
+            const int g2 = comp == 0 ? 2 : (comp == 1 ? 4 : 5);
+            auto ld_green = [&](int pos) {
+                const T2 X = lx[pos], Y = ly[pos], Z = lz[pos];
+                const T a0g = gsm[((size_t)g0 * N + pos) * TX + c];
+                const T a1g = gsm[((size_t)g1 * N + pos) * TX + c];
+                const T a2g = gsm[((size_t)g2 * N + pos) * TX + c];
+                return cmk<T2>(a0g * X.x + a1g * Y.x + a2g * Z.x, a0g * X.y + a1g * Y.y + a2g * Z.y);
+            };
+            stage_a<R2, R1, +1, TPL, true>(my, t, act, tw, ld_green);  // CTA barrier
+        }
+        gbar();
+        {
+            T2* base = reinterpret_cast<T2*>(a0.group[m].spec) + comp * a0.nh + ky * a0.rs + k0 +
+                       (act ? c : 0);
+            const long long es = a0.plane;
+            auto st_g = [&](int pos, T2 v) { base[pos * es] = v; };
+            stage_b<R2, R1, +1, TPL, false>(my, t, act, st_g);
+        }
+        __syncthreads();  // this stage and, after the tile's last member, this Green buffer are refilled
+    }
+}
+
+
 }  // namespace fast
 
 // Runs the five passes with the specialised kernels when the grid, the
@@ -768,11 +894,12 @@ cudaError_t fast_apply(Problem& P, int precision, const ApplyArgs& aa, int* npar
 // group must share (kGroupGeometry values); fast_apply_group launches the five
 // passes over `members` members whose arguments and maps the caller copied to
 // device memory (d_args[members], d_maps[2 * members], 64-byte aligned).
+// shared_green: every member's Green map is member 0's (k_fz_shared).
 constexpr int kGroupGeometry = 12;
 cudaError_t fast_member_args(Problem& P, int precision, const ApplyArgs& aa, fast::FastArgs* args,
                              CUtensorMap* maps, long long* geometry);
 cudaError_t fast_apply_group(Problem& P0, int precision, int members, const fast::FastArgs* d_args,
-                             const CUtensorMap* d_maps, int* nparts);
+                             const CUtensorMap* d_maps, bool shared_green, int* nparts);
 
 }  // namespace fp
 
@@ -853,6 +980,8 @@ struct Passes {
     static cudaError_t y(int dir, const FastArgs& a, dim3 grid, cudaStream_t s);
     static cudaError_t z(int stages, const CUtensorMap& spec_map, const CUtensorMap& green_map,
                          const FastArgs& a, dim3 grid, size_t smem, cudaStream_t s);
+    // the group z pass with one shared Green table (a.share members)
+    static cudaError_t z_shared(const FastArgs& a, int grid, size_t smem, cudaStream_t s);
     // blocks resident per SM at this shared-memory size
     static int z_per_sm(int stages, size_t smem);
     static int x_per_sm(bool inverse, int threads, size_t smem);
@@ -868,6 +997,8 @@ cudaError_t run_y(int n, int dir, const FastArgs& a, dim3 grid, cudaStream_t s);
 template <typename T>
 cudaError_t run_z(int n, int stages, const CUtensorMap& spec_map, const CUtensorMap& green_map,
                   const FastArgs& a, dim3 grid, size_t smem, cudaStream_t s);
+template <typename T>
+cudaError_t run_z_shared(int n, const FastArgs& a, int grid, size_t smem, cudaStream_t s);
 // blocks of the z kernel resident per SM at this shared-memory size
 template <typename T>
 int z_blocks_per_sm(int n, int stages, size_t smem);

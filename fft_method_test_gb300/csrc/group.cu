@@ -95,15 +95,17 @@ cudaError_t group_iterations(Problem* const* m, int members, int count, GroupTab
             return cudaErrorInvalidValue;
     }
     // The Green table depends only on the grid, voxel size, viscosity and
-    // alias radius: members that share them all read member 0's table (one
-    // table in L2 for the group; at 256^3 the members' z passes run one after
-    // another, so this saves memory traffic only on small grids, where the
-    // members' z-pass CTAs are resident together).
+    // alias radius: members that share them all read member 0's table, and
+    // when all of them do, the z pass (k_fz_shared) loads each Green tile
+    // once for the whole group.
+    bool shared_green = true;
     for (int p = 1; p < members; ++p) {
         const Problem& P = *m[p];
         if (P.h == P0.h && P.mu == P0.mu && P.p_radius == P0.p_radius) {
             base[(size_t)p].green = base[0].green;
             t->h_maps[2 * p + 1] = t->h_maps[1];
+        } else {
+            shared_green = false;
         }
     }
     const int nparts = (int)geom0[7];  // partial rows of the inverse x pass
@@ -137,7 +139,8 @@ cudaError_t group_iterations(Problem* const* m, int members, int count, GroupTab
         return e;
     for (int i = 0; i < count; ++i) {
         int np = 0;
-        e = fast_apply_group(P0, prec, members, t->d_fast + (size_t)i * members, t->d_maps, &np);
+        e = fast_apply_group(P0, prec, members, t->d_fast + (size_t)i * members, t->d_maps, shared_green,
+                             &np);
         if (e != cudaSuccess) return e;
         e = group_iteration_tail(s, t->d_iter + (size_t)i * members, members, max_blocks);
         if (e != cudaSuccess) return e;
