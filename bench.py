@@ -72,8 +72,8 @@ def parse():
     ap.add_argument("--precision", default="mixed,fp64", help="precisions for --mode apply")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--tiling", default="",
-                    help="--mode apply: 'auto' (autotune) or 'tile,tma,x_bulk,x_rows[,lowreg]' "
-                         "(e.g. 8,0,1,0)")
+                    help="--mode apply / solve: 'auto' (autotune; the default of solve) or "
+                         "'tile,tma,x_bulk,x_rows[,lowreg]' (e.g. 16,1,1,4,0)")
     ap.add_argument("--batch-count", type=int, default=64, help="microstructures for --mode batch")
     ap.add_argument("--concurrency", type=int, default=8, help="host threads for --mode batch")
     ap.add_argument("--max-group", type=int, default=16,
@@ -355,7 +355,14 @@ def run_ours(args, world, rank, local):
     # the analogue of the reference's FFTW_MEASURE planning; untimed here,
     # its wall time is reported with e2e
     t0 = time.perf_counter()
-    tuned = prob.autotune()
+    if args.tiling and args.tiling != "auto":
+        # a fixed tiling (e.g. the tuner's choice of an earlier run), for
+        # profilers: the tuner's timings are not meaningful under ncu
+        t, tma, xb, xr, lo = (int(v) for v in (args.tiling + ",0").split(",")[:5])
+        prob.set_tiling(t, bool(tma), bool(xb), xr, bool(lo))
+        tuned = dict(tile=t, tma=bool(tma), x_bulk=bool(xb), x_rows=xr, lowreg=bool(lo), fixed=True)
+    else:
+        tuned = prob.autotune()
     t_tune = time.perf_counter() - t0
 
     # FP64 reference solve on the same cell (plain FP64 GPU MINRES)
@@ -473,7 +480,11 @@ def run_ours(args, world, rank, local):
         t0 = time.perf_counter()
         with PermeabilityProblem(mask.shape, precision="mixed") as p2:
             p2.set_geometry(mask_c)
-            p2.autotune()  # the cached tiling of this grid
+            if tuned.get("fixed"):
+                p2.set_tiling(tuned["tile"], tuned["tma"], tuned["x_bulk"], tuned["x_rows"],
+                              tuned["lowreg"])
+            else:
+                p2.autotune()  # the cached tiling of this grid
             K2, _ = p2.solve_permeability(TOL_MIXED, MAXIT, block=True)
         e2e_times.append(time.perf_counter() - t0)
     e2e = max_over_ranks(world, float(np.mean(e2e_times)))
