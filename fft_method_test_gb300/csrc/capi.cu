@@ -1081,6 +1081,10 @@ int fp_group_solve_permeability(int count, fp_handle* handles, double tol, int64
         if (P.nx != P0.nx || P.ny != P0.ny || P.nz != P0.nz || P.precision != P0.precision ||
             P.reliable_interval != P0.reliable_interval)
             return fail(P, FP_ERR_INVALID, "group: members must share grid, precision and reliable interval");
+        if (P.tile_yz != P0.tile_yz || P.tma_off != P0.tma_off || P.x_bulk != P0.x_bulk ||
+            P.x_rows != P0.x_rows || P.yz_lowreg != P0.yz_lowreg || P.fast_off != P0.fast_off)
+            return fail(P, FP_ERR_INVALID,
+                        "group: members must share the FFT tiling (fp_autotune or fp_set_tiling on each)");
     }
     bool grouped = count > 1;
     for (int i = 0; i < count && grouped; ++i) grouped = fp::group_supported(handles[i]->P);

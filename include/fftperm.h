@@ -226,8 +226,8 @@ int fp_batch_solve_grouped(int count, const int* dims, const uint8_t* const* mas
                            int max_group, double* K, fp_solver_stats* stats, int* status);
 const char* fp_batch_last_error(void);
 
-/* K of several problems of one grid (same dimensions, precision and reliable
- * interval) solved together: the three load cases in turn, each as one
+/* K of several problems of one grid (same dimensions, precision, reliable
+ * interval and FFT tiling; FP_ERR_INVALID otherwise) solved together: the three load cases in turn, each as one
  * lockstep MINRES over the members with one kernel launch per FFT pass and
  * per vector kernel for all of them (no reference counterpart: the reference
  * runs PermeabilityRunner::run once per geometry, src/app/PermeabilityRunner.cpp:451).

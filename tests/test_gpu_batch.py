@@ -197,6 +197,19 @@ def test_group_rejects_mixed_grids(gpu_lib):
             p.close()
 
 
+def test_group_rejects_different_tilings(gpu_lib):
+    from fft_method_test_gb300.permeability import group_solve_permeability
+
+    ps = _problems(_group_masks(32)[:2], "mixed")
+    try:
+        ps[1].set_tiling(8, True, True, 2, False)
+        with pytest.raises(ValueError, match="tiling"):
+            group_solve_permeability(ps, 1e-7)
+    finally:
+        for p in ps:
+            p.close()
+
+
 def test_grouped_batch_equals_ungrouped(gpu_lib):
     """fp_batch_solve_grouped (groups of up to 3 per grid) against the
     ungrouped batch: identical K and iterations; uneven group sizes."""
