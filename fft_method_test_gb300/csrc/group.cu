@@ -8,7 +8,11 @@
 // kernels_minres.cu) take their member from blockIdx.  A member whose solve
 // is done returns at the top of every kernel through its own stop flag.  The
 // x passes keep each member's own grid and the vector kernels its own block
-// count, so every member computes exactly what it computes alone.
+// count, so every member computes exactly what it computes alone.  When all
+// members share one Green table (same grid, voxel size, viscosity and alias
+// radius), the z pass is k_fz_shared, which loads each Green tile once for
+// all members (and transforms a done member's stale spectrum, which nothing
+// reads, rather than skip it).
 #include <cuda_runtime.h>
 
 #include <algorithm>
