@@ -271,7 +271,7 @@ int read_scalars(Problem& P) {
 // |r0 - A32 (x - x0)| is recomputed (reliable update).  A segment ends when
 // the recurrence reports convergence or breakdown, when that true residual is
 // below tol, or when the recurrence estimate has run ahead of it (below
-// P.ahead_factor = 0.85 of it).  The FP64 residual |b - A x| then decides:
+// P.ahead_factor = 0.95 of it).  The FP64 residual |b - A x| then decides:
 // below tol the solve has converged, otherwise a new segment starts from x.  The reported
 // residual is that FP64 residual; the history holds the last segment.
 // State of one MINRES solve between chunks of iterations: device_minres runs
