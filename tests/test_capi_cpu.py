@@ -44,6 +44,27 @@ def test_python_mirror_loads_and_validates_without_gpu():
         t.set_column(3, [0, 0, 0])
 
 
+def test_group_and_batch_entries_reject_bad_arguments_without_gpu():
+    """The group, block and grouped-batch entries check their arguments before
+    any CUDA call (status FP_ERR_INVALID)."""
+    import ctypes as C
+
+    from fft_method_test_gb300 import _capi
+    from fft_method_test_gb300.permeability import batch_solve_permeability
+
+    lib = _capi.load()
+    K = np.zeros(9)
+    assert lib.fp_group_solve_permeability(0, None, 1e-7, 100, K, None) == _capi.FP_ERR_INVALID
+    hs = (C.c_void_p * 2)(None, None)
+    assert lib.fp_group_solve_permeability(2, hs, 1e-7, 100, K, None) == _capi.FP_ERR_INVALID
+    assert lib.fp_solve_permeability_block(None, 1e-7, 100, K, None) == _capi.FP_ERR_INVALID
+    mask = np.ones((8, 8, 8), np.uint8)
+    with pytest.raises(ValueError):
+        batch_solve_permeability([mask], max_group=0)
+    with pytest.raises(ValueError):
+        batch_solve_permeability([mask], concurrency=0, max_group=4)
+
+
 @pytest.mark.parametrize("precision", ["FFT_METHOD_PRECISION_DOUBLE", "FFT_METHOD_PRECISION_FLOAT"])
 def test_cpp_adapters_compile_against_reference(precision):
     """The C++ drop-ins (CudaFFTBackend : IFFTBackend, CudaVariationalOperator :
