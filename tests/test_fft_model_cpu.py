@@ -106,3 +106,39 @@ def test_prime_factor_dft(p, q):
     v = np.random.default_rng(p * q).standard_normal(p * q) + 0.5j
     np.testing.assert_allclose(_dft_pfa(v, p, q, -1), np.fft.fft(v), atol=1e-12)
     np.testing.assert_allclose(_dft_pfa(v, p, q, +1), p * q * np.fft.ifft(v), atol=1e-12)
+
+
+@pytest.mark.parametrize("n", [32, 48, 80, 160, 256])
+def test_two_real_lines_separation_and_reconstruction(n):
+    """k_fx_fwd: one complex FFT of z = a + i b gives both half spectra,
+    A[k] = (Z[k] + conj Z[-k]) / 2 and B[k] = (Z[k] - conj Z[-k]) / (2i), for
+    k = 0 .. N/2 + 1 (the last lands in the row padding).  k_fx_inv: Z[k] =
+    A[k] + i B[k] below N/2 + 1 and conj A[N-k] + i conj B[N-k] above, with
+    the DC and Nyquist imaginary parts dropped; the inverse FFT returns a and
+    b as its real and imaginary parts."""
+    rng = np.random.default_rng(n)
+    a, b = rng.standard_normal(n), rng.standard_normal(n)
+    Z = np.fft.fft(a + 1j * b)
+    nh = n // 2 + 1
+    A = np.empty(nh + 1, complex)
+    B = np.empty(nh + 1, complex)
+    for k in range(nh + 1):  # the kernel's pairs run to k = NH (even count)
+        zk, zn = Z[k], Z[0 if k == 0 else n - k]
+        A[k] = complex(0.5 * (zk.real + zn.real), 0.5 * (zk.imag - zn.imag))
+        B[k] = complex(0.5 * (zk.imag + zn.imag), 0.5 * (zn.real - zk.real))
+    np.testing.assert_allclose(A[:nh], np.fft.rfft(a), atol=1e-10)
+    np.testing.assert_allclose(B[:nh], np.fft.rfft(b), atol=1e-10)
+    # reconstruction from the stored half spectra (positions 0 .. N/2 only)
+    Zr = np.empty(n, complex)
+    for k in range(n):
+        lo = k < nh
+        kk = k if lo else n - k
+        Ak, Bk = complex(A[kk]), complex(B[kk])
+        if kk == 0 or 2 * kk == n:
+            Ak, Bk = complex(Ak.real, 0.0), complex(Bk.real, 0.0)
+        if not lo:
+            Ak, Bk = Ak.conjugate(), Bk.conjugate()
+        Zr[k] = complex(Ak.real - Bk.imag, Ak.imag + Bk.real)
+    z = np.fft.ifft(Zr)
+    np.testing.assert_allclose(z.real, a, atol=1e-12)
+    np.testing.assert_allclose(z.imag, b, atol=1e-12)
